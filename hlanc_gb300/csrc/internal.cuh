@@ -1,0 +1,166 @@
+// internal.cuh -- device data model of the GB300 IRLM engine.
+//
+// One solve (or one member of a batch) is a "problem".  Everything the
+// implicitly restarted Lanczos loop touches lives in HBM for the whole solve:
+//   V      ld x ncv FP64 basis, column-major, ld = n rounded up to 64 rows
+//          (512-byte aligned columns; padding rows stay zero),
+//   r0/r1  residual ping-pong (step j reads r[j&1], writes r[(j+1)&1]),
+//   small  the ncv-sized arrays of the reference's workl (T, Ritz values,
+//          bounds, Q), see the SM_* offsets,
+//   State  scalars (rnorm, wnorm, DGKS flags, nev/np, status).
+// Rows are split into tiles (multiples of 64 rows); every row-parallel kernel
+// runs one CTA per tile and reduces its partial sums deterministically: each
+// tile writes a fixed slot, the last CTA to finish sums the slots in tile
+// order.  A batch is simply several problems whose tiles share one launch.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/hlanc_gb300.h"
+
+namespace hlanc {
+
+constexpr int TPB = 256;                 // threads per CTA of the tile kernels
+constexpr int ROW_ALIGN = 64;            // tile boundaries / ld granularity
+constexpr int MAXNCV = HLANC_MAX_NCV;
+constexpr int LONG_ROW = 96;             // rows longer than this are reduced by a warp
+
+enum : int { ST_RUNNING = 0, ST_CONVERGED = 1, ST_NOT_CONVERGED = 2, ST_FAILED = 3 };
+enum : int { PH_EXTEND = 0, PH_APPLY = 1, PH_DONE = 2 };
+
+struct State {
+    int status;            // ST_*
+    int phase;             // PH_*
+    int k, np, nev;        // current extension runs steps j = k .. k+np-1; nev after adjustment
+    int iter;              // restart cycles completed (ds_solver loop counter)
+    int nconv;
+    int need2, need3;      // DGKS second / third pass needed for the current step
+    int max_iter;
+    int nev0, np0, ncv;
+    int err;               // device-detected inconsistency (never expected)
+    double rnorm, wnorm;
+    double tol, eps23;
+    long long spmv, passes;
+    long long sumc;        // sum over CGS passes of the column count c (algorithmic bytes)
+    long long sumnev;      // sum over applied restarts of nev (algorithmic bytes)
+    int napply;            // restarts applied to V
+    int fin;               // 0 = not finalised, 1 = Qfull/values ready, 2 = Ritz vectors written
+    int pad1;
+};
+
+// offsets (in doubles) of the per-problem small arrays, m = ncv
+__host__ __device__ inline int SM_H(int)        { return 0; }           // h[j]=beta_j, h[m+j]=alpha_j
+__host__ __device__ inline int SM_HV(int m)     { return 2 * m; }       // projection coefficients
+__host__ __device__ inline int SM_RITZ(int m)   { return 3 * m; }
+__host__ __device__ inline int SM_BOUNDS(int m) { return 4 * m; }
+__host__ __device__ inline int SM_RITZS(int m)  { return 5 * m; }       // last-iteration snapshot (workl+ncv)
+__host__ __device__ inline int SM_BNDS(int m)   { return 6 * m; }       // (workl+2ncv)
+__host__ __device__ inline int SM_VALS(int m)   { return 7 * m; }       // final eigenvalues
+__host__ __device__ inline int SM_WORK(int m)   { return 8 * m; }       // 4m scratch
+__host__ __device__ inline int SM_Q(int m)      { return 12 * m; }      // m*m (dsapps Q / eigvecs of T)
+__host__ __device__ inline int SM_Q2(int m)     { return 12 * m + m * m; }  // m*m (final Householder Q)
+__host__ __device__ inline int SM_SIZE(int m)   { return 12 * m + 2 * m * m; }
+
+struct Problem {
+    // operator (general CSR on the device)
+    const int *row_ptr;
+    const int *col;
+    const double *val;
+    const float *val32;    // FP32 values (mixed precision), or null
+    float *x32;            // FP32 copy of the current Lanczos vector
+    int n, ld, ncv, nev0;
+    int tile0, ntiles;
+    int fp32;              // SpMV on FP32 values/vectors
+    int pstride;           // doubles per tile partial slot
+    double *V;
+    double *r0, *r1;
+    double *part;
+    unsigned *counter;
+    State *st;
+    double *small;
+    const double *wext;    // non-null: operator output is supplied by the host callback path
+    double *vout;          // Ritz vectors destination (device, ldo x ncv)
+    int ldo, pad2;
+};
+
+struct Tile { int prob, row0, row1, pad; };
+
+// ---- device helpers --------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Write this tile's nv partial sums (smem `mine`) to its slot, then let the
+// last CTA of the problem sum all slots in tile order into smem `total`.
+// Returns true (in every thread of that CTA) for the last CTA only.
+__device__ __forceinline__ bool finish_tile(const Problem &P, int tl, int nv, const double *mine,
+                                            double *total) {
+    __shared__ unsigned s_ticket;
+    double *slot = P.part + (size_t)tl * P.pstride;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) slot[i] = mine[i];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_ticket = atomicAdd(P.counter, 1u);
+    __syncthreads();
+    if (s_ticket != (unsigned)(P.ntiles - 1)) return false;
+    __threadfence();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i = warp; i < nv; i += nw) {
+        double s = 0.0;
+        for (int t = lane; t < P.ntiles; t += 32) s += __ldcg(P.part + (size_t)t * P.pstride + i);
+        s = warp_sum(s);
+        if (lane == 0) total[i] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *P.counter = 0u;
+    return true;
+}
+
+// CTA-wide sum of one value per thread (deterministic), result in every thread.
+__device__ __forceinline__ double block_sum(double v, double *scratch /* >= 32 */) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += scratch[w];
+    return s;
+}
+
+__device__ __forceinline__ const double *step_in(const Problem &P, int j) { return (j & 1) ? P.r1 : P.r0; }
+__device__ __forceinline__ double *step_out(const Problem &P, int j) { return (j & 1) ? P.r0 : P.r1; }
+
+// ---- kernel entry points (kernels_step.cu / kernels_restart.cu) -----------
+void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, int prob,
+                         unsigned long long seed, cudaStream_t s);
+void launch_norm_init(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s);
+void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, bool fp32_any,
+                 bool external_w, cudaStream_t s);
+void launch_prep_f32(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, cudaStream_t s);
+void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, double *xout,
+                     cudaStream_t s);
+void launch_restart(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
+void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, int max_nev,
+                  cudaStream_t s);
+void launch_finalize(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
+void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, cudaStream_t s);
+void launch_spmv(const int *row_ptr, const int *col, const double *val, int nrows, const double *x,
+                 double *y, cudaStream_t s);
+void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, int nrows,
+                     const float *x, float *y, cudaStream_t s);
+void launch_residuals(const int *row_ptr, const int *col, const double *val, int n, int k,
+                      const double *values_d, const double *vectors_d, int ldv, double *out4k,
+                      cudaStream_t s);
+
+long long &launch_counter();
+
+}  // namespace hlanc

@@ -1,0 +1,461 @@
+// kernels_step.cu -- row-parallel kernels of one Lanczos step (HLanc.hpp:1410-1477)
+//
+// A step j of the reference's dsaitr is, on the device:
+//   k_spmv   v_j = r / rnorm -> V[:, j];  w = A v_j            (FP64 or FP32 SpMV)
+//   k_proj   h = V[:, 0:j+1]^T w  (+ ||w||^2 on the first pass)   CGS projection
+//   k_apply  w -= V[:, 0:j+1] h,  ||w||^2 -> rnorm, DGKS test      CGS update
+//   k_proj / k_apply again while the DGKS test (factor 0.717) asks for it.
+// All decisions (second/third pass, invariant-subspace reset) are taken on
+// the device by the last CTA of each kernel, so a whole restart cycle runs
+// without host synchronisation and can be captured in one CUDA graph.
+//
+// GB300 note: these kernels stream V once per pass with one FP64 FMA per
+// element.  Blackwell Ultra's FP64 rate is low, so each inner loop issues
+// exactly one DFMA per loaded element and every reduction is accumulated in
+// registers over a whole tile before the (few) shuffle additions.
+#include <float.h>
+
+#include "internal.cuh"
+
+namespace hlanc {
+
+long long &launch_counter() {
+    static long long c = 0;
+    return c;
+}
+
+// ---- SplitMix64 start vector (same formula as generators.start_vector) ----
+__host__ __device__ inline uint64_t sm_mix(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(TPB) k_start(const Problem *__restrict__ probs,
+                                               const Tile *__restrict__ tiles, int prob,
+                                               unsigned long long key) {
+    const Tile t = tiles[blockIdx.x];
+    if (t.prob != prob) return;
+    const Problem &P = probs[t.prob];
+    for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
+        uint64_t x = sm_mix(key + (uint64_t)(r + 1) * 0x9E3779B97F4A7C15ULL);
+        double u = (double)(x >> 11) * 0x1.0p-53;
+        P.r0[r] = 2.0 * u - 1.0;
+    }
+}
+
+// rnorm = ||r0|| for problems in the initial phase (dgetv0, HLanc.hpp:1373)
+__global__ void __launch_bounds__(TPB) k_norm_init(const Problem *__restrict__ probs,
+                                                   const Tile *__restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Problem &P = probs[t.prob];
+    if (P.st->iter != -1) return;   // -1 marks "start vector written, norm pending"
+    __shared__ double scratch[32], mine[1], tot[1];
+    double s = 0.0;
+    for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) s = fma(P.r0[r], P.r0[r], s);
+    s = block_sum(s, scratch);
+    if (threadIdx.x == 0) mine[0] = s;
+    __syncthreads();
+    if (!finish_tile(P, blockIdx.x - P.tile0, 1, mine, tot)) return;
+    if (threadIdx.x == 0) {
+        P.st->rnorm = sqrt(tot[0]);
+        P.st->iter = 0;
+    }
+}
+
+__device__ __forceinline__ bool step_active(const State *S, int s) {
+    return S->status == ST_RUNNING && S->phase == PH_EXTEND && s < S->np;
+}
+
+// ---- SpMV of the step --------------------------------------------------------
+// Thread per row (one DFMA per stored entry, no shuffles); rows longer than
+// LONG_ROW are deferred and reduced by a whole warp.
+template <bool F32>
+__global__ void __launch_bounds__(TPB) k_spmv_step(const Problem *__restrict__ probs,
+                                                   const Tile *__restrict__ tiles, int s) {
+    const Tile t = tiles[blockIdx.x];
+    const Problem &P = probs[t.prob];
+    const State *S = P.st;
+    if ((bool)P.fp32 != F32 || P.wext) return;
+    if (!step_active(S, s)) return;
+    const int j = S->k + s;
+    const double rn = S->rnorm;
+    const bool scale = rn > DBL_MIN;
+    const double t1 = scale ? 1.0 / rn : 1.0;
+    const double *__restrict__ rin = step_in(P, j);
+    double *__restrict__ w = step_out(P, j);
+    double *__restrict__ vj = P.V + (size_t)j * P.ld;
+    const int *__restrict__ rp = P.row_ptr;
+    const int *__restrict__ ci = P.col;
+    __shared__ int s_long[TPB];
+    __shared__ int s_nlong;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int base = t.row0; base < t.row1; base += TPB) {
+        if (threadIdx.x == 0) s_nlong = 0;
+        __syncthreads();
+        const int r = base + threadIdx.x;
+        if (r < t.row1) {
+            if (!F32) {
+                const double x = rin[r];
+                vj[r] = scale ? x * t1 : x;
+            }
+            const int a = rp[r], b = rp[r + 1];
+            if (b - a > LONG_ROW) {
+                s_long[atomicAdd(&s_nlong, 1)] = r;
+            } else if (F32) {
+                const float *__restrict__ v32 = P.val32;
+                const float *__restrict__ x32 = P.x32;
+                float acc = 0.f;
+                for (int i = a; i < b; ++i) acc = fmaf(v32[i], x32[ci[i]], acc);
+                w[r] = (double)acc;
+            } else {
+                const double *__restrict__ val = P.val;
+                double acc = 0.0;
+                for (int i = a; i < b; ++i) acc = fma(val[i], rin[ci[i]], acc);
+                w[r] = scale ? acc * t1 : acc;
+            }
+        }
+        __syncthreads();
+        for (int q = warp; q < s_nlong; q += TPB / 32) {
+            const int rr = s_long[q];
+            const int a = rp[rr], b = rp[rr + 1];
+            if (F32) {
+                float acc = 0.f;
+                for (int i = a + lane; i < b; i += 32) acc = fmaf(P.val32[i], P.x32[ci[i]], acc);
+                acc = warp_sum_f(acc);
+                if (lane == 0) w[rr] = (double)acc;
+            } else {
+                double acc = 0.0;
+                for (int i = a + lane; i < b; i += 32) acc = fma(P.val[i], rin[ci[i]], acc);
+                acc = warp_sum(acc);
+                if (lane == 0) w[rr] = scale ? acc * t1 : acc;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// v_j -> V[:, j] (and its FP32 copy) ahead of an FP32 SpMV or a host operator.
+__global__ void __launch_bounds__(TPB) k_prep(const Problem *__restrict__ probs,
+                                              const Tile *__restrict__ tiles, int s, int ext,
+                                              double *__restrict__ xout) {
+    const Tile t = tiles[blockIdx.x];
+    const Problem &P = probs[t.prob];
+    const State *S = P.st;
+    if (ext ? !P.wext : !P.fp32) return;
+    if (!step_active(S, s)) return;
+    const int j = S->k + s;
+    const double rn = S->rnorm;
+    const bool scale = rn > DBL_MIN;
+    const double t1 = scale ? 1.0 / rn : 1.0;
+    const double *__restrict__ rin = step_in(P, j);
+    double *__restrict__ vj = P.V + (size_t)j * P.ld;
+    for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
+        const double x = rin[r];
+        const double v = scale ? x * t1 : x;
+        vj[r] = v;
+        if (ext) xout[r] = v;
+        else P.x32[r] = (float)v;
+    }
+}
+
+// ---- CGS projection: h = V[:, 0:c)^T w  (+ ||w||^2 on pass 1) ----------------
+// Warp w owns columns k = w, w+8, ...; lane l owns rows l and l+32 of every
+// 64-row chunk.  Accumulators stay in registers for the whole tile.
+__global__ void __launch_bounds__(TPB) k_proj(const Problem *__restrict__ probs,
+                                              const Tile *__restrict__ tiles, int s, int pass) {
+    const Tile t = tiles[blockIdx.x];
+    const Problem &P = probs[t.prob];
+    State *S = P.st;
+    if (!step_active(S, s)) return;
+    if ((pass == 2 && !S->need2) || (pass == 3 && !S->need3)) return;
+    const int j = S->k + s;
+    const int c = j + 1;
+    const int m = P.ncv;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double *__restrict__ w = step_out(P, j);
+    const size_t ld = (size_t)P.ld;
+    double acc[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) acc[i] = 0.0;
+    double nrm = 0.0;
+    for (int r = t.row0; r < t.row1; r += 64) {
+        const double w0 = w[r + lane];
+        const double w1 = w[r + 32 + lane];
+        if (pass == 1 && warp == 0) {
+            nrm = fma(w0, w0, nrm);
+            nrm = fma(w1, w1, nrm);
+        }
+        const double *__restrict__ vb = P.V + r + lane;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int k = warp + 8 * i;
+            if (k < c) {
+                const double *vk = vb + (size_t)k * ld;
+                acc[i] = fma(__ldcs(vk), w0, acc[i]);
+                acc[i] = fma(__ldcs(vk + 32), w1, acc[i]);
+            }
+        }
+    }
+    __shared__ double red[MAXNCV + 1], tot[MAXNCV + 1];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int k = warp + 8 * i;
+        if (k < c) {
+            const double v = warp_sum(acc[i]);
+            if (lane == 0) red[k] = v;
+        }
+    }
+    if (pass == 1 && warp == 0) {
+        nrm = warp_sum(nrm);
+        if (lane == 0) red[c] = nrm;
+    }
+    __syncthreads();
+    if (!finish_tile(P, blockIdx.x - P.tile0, c + (pass == 1 ? 1 : 0), red, tot)) return;
+    double *h = P.small + SM_H(m);
+    double *hv = P.small + SM_HV(m);
+    for (int i = threadIdx.x; i < c; i += TPB) hv[i] = tot[i];
+    if (threadIdx.x == 0) {
+        if (pass == 1) {
+            h[m + j] = tot[j];                       // alpha_j, HLanc.hpp:1433
+            h[j] = (j == 0) ? 0.0 : S->rnorm;         // beta_j,  HLanc.hpp:1434-1438
+            S->wnorm = sqrt(tot[c]);                  // HLanc.hpp:1429
+            S->spmv += 1;
+        } else {
+            h[m + j] += tot[j];                       // HLanc.hpp:1447
+        }
+        S->passes += 1;
+    }
+}
+
+// ---- CGS update: w -= V[:, 0:c) h ; DGKS decision ------------------------------
+__global__ void __launch_bounds__(TPB) k_apply(const Problem *__restrict__ probs,
+                                               const Tile *__restrict__ tiles, int s, int pass) {
+    const Tile t = tiles[blockIdx.x];
+    const Problem &P = probs[t.prob];
+    State *S = P.st;
+    if (!step_active(S, s)) return;
+    if ((pass == 2 && !S->need2) || (pass == 3 && !S->need3)) return;
+    const int j = S->k + s;
+    const int c = j + 1;
+    const int m = P.ncv;
+    double *__restrict__ w = step_out(P, j);
+    __shared__ double hs[MAXNCV];
+    __shared__ double scratch[32], mine[1], tot[1];
+    __shared__ int s_zero;
+    const double *hv = P.small + SM_HV(m);
+    for (int i = threadIdx.x; i < c; i += TPB) hs[i] = hv[i];
+    __syncthreads();
+    const size_t ld = (size_t)P.ld;
+    double nrm = 0.0;
+    for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
+        const double *__restrict__ vr = P.V + r;
+        double acc = w[r];
+        int k = 0;
+        for (; k + 8 <= c; k += 8) {
+            double v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc = fma(-v[q], hs[k + q], acc);
+        }
+        for (; k < c; ++k) acc = fma(-__ldcs(vr + (size_t)k * ld), hs[k], acc);
+        w[r] = acc;
+        nrm = fma(acc, acc, nrm);
+    }
+    nrm = block_sum(nrm, scratch);
+    if (threadIdx.x == 0) mine[0] = nrm;
+    __syncthreads();
+    if (!finish_tile(P, blockIdx.x - P.tile0, 1, mine, tot)) return;
+    if (threadIdx.x == 0) {
+        const double nr = sqrt(tot[0]);
+        s_zero = 0;
+        S->sumc += c;
+        if (pass == 1) {                               // HLanc.hpp:1440-1444
+            S->rnorm = nr;
+            S->need2 = nr < S->wnorm * 0.717;
+            S->need3 = 0;
+        } else if (pass == 2) {                        // HLanc.hpp:1450-1458
+            S->need3 = !(nr > S->rnorm * 0.717);
+            S->rnorm = nr;
+        } else {                                       // HLanc.hpp:1450-1463
+            if (nr > S->rnorm * 0.717) {
+                S->rnorm = nr;
+            } else {
+                S->rnorm = 0.0;
+                s_zero = 1;
+            }
+        }
+    }
+    __syncthreads();
+    if (s_zero)   // invariant subspace: resid = 0 (rare; one CTA clears the vector)
+        for (int r = threadIdx.x; r < P.n; r += TPB) w[r] = 0.0;
+}
+
+// ---- standalone SpMV (operator() of dcsrmv_operator_gpu) -------------------
+template <typename T>
+__global__ void __launch_bounds__(TPB) k_spmv_plain(const int *__restrict__ rp,
+                                                    const int *__restrict__ ci,
+                                                    const T *__restrict__ val, int nrows,
+                                                    const T *__restrict__ x, T *__restrict__ y) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ int s_long[TPB];
+    __shared__ int s_nlong;
+    for (int base = blockIdx.x * TPB; base < nrows; base += gridDim.x * TPB) {
+        if (threadIdx.x == 0) s_nlong = 0;
+        __syncthreads();
+        const int r = base + threadIdx.x;
+        if (r < nrows) {
+            const int a = rp[r], b = rp[r + 1];
+            if (b - a > LONG_ROW) {
+                s_long[atomicAdd(&s_nlong, 1)] = r;
+            } else {
+                T acc = T(0);
+                for (int i = a; i < b; ++i) acc = fma(val[i], x[ci[i]], acc);
+                y[r] = acc;
+            }
+        }
+        __syncthreads();
+        for (int q = warp; q < s_nlong; q += TPB / 32) {
+            const int rr = s_long[q];
+            const int a = rp[rr], b = rp[rr + 1];
+            T acc = T(0);
+            for (int i = a + lane; i < b; i += 32) acc = fma(val[i], x[ci[i]], acc);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) y[rr] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- residuals of k Ritz pairs (demo/verify_eigs.cu:52-98) ------------------
+// out4k[4*i + 0] = ||A v - lambda v||^2, +1 = max|Av - lambda v|, +2 = max|Av|, +3 = max|lambda v|
+__global__ void __launch_bounds__(TPB) k_residuals(const int *__restrict__ rp,
+                                                   const int *__restrict__ ci,
+                                                   const double *__restrict__ val, int n,
+                                                   const double *__restrict__ values,
+                                                   const double *__restrict__ V, int ldv,
+                                                   double *__restrict__ part) {
+    const int i = blockIdx.y;
+    const double lam = values[i];
+    const double *v = V + (size_t)i * ldv;
+    double ss = 0.0, md = 0.0, ma = 0.0, mb = 0.0;
+    for (int r = blockIdx.x * TPB + threadIdx.x; r < n; r += gridDim.x * TPB) {
+        double acc = 0.0;
+        for (int q = rp[r]; q < rp[r + 1]; ++q) acc = fma(val[q], v[ci[q]], acc);
+        const double lv = lam * v[r];
+        const double d = acc - lv;
+        ss = fma(d, d, ss);
+        md = fmax(md, fabs(d));
+        ma = fmax(ma, fabs(acc));
+        mb = fmax(mb, fabs(lv));
+    }
+    __shared__ double sh[4][TPB / 32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    ss = warp_sum(ss);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+        ma = fmax(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+        mb = fmax(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+    }
+    if (lane == 0) { sh[0][warp] = ss; sh[1][warp] = md; sh[2][warp] = ma; sh[3][warp] = mb; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0, c = 0, d = 0;
+        for (int q = 0; q < TPB / 32; ++q) { a += sh[0][q]; b = fmax(b, sh[1][q]); c = fmax(c, sh[2][q]); d = fmax(d, sh[3][q]); }
+        double *o = part + ((size_t)i * gridDim.x + blockIdx.x) * 4;
+        o[0] = a; o[1] = b; o[2] = c; o[3] = d;
+    }
+}
+
+__global__ void k_residuals_final(const double *__restrict__ part, int nblk, int k,
+                                  double *__restrict__ out4k) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    double a = 0, b = 0, c = 0, d = 0;
+    for (int q = 0; q < nblk; ++q) {
+        const double *o = part + ((size_t)i * nblk + q) * 4;
+        a += o[0]; b = fmax(b, o[1]); c = fmax(c, o[2]); d = fmax(d, o[3]);
+    }
+    out4k[4 * i + 0] = a; out4k[4 * i + 1] = b; out4k[4 * i + 2] = c; out4k[4 * i + 3] = d;
+}
+
+// ---- launchers --------------------------------------------------------------
+void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, int prob,
+                         unsigned long long seed, cudaStream_t s) {
+    const unsigned long long key = sm_mix(seed * 0xD1B54A32D192ED03ULL + 0ULL);
+    k_start<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, prob, key);
+    launch_counter() += 1;
+}
+
+void launch_norm_init(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s) {
+    k_norm_init<<<ntiles, TPB, 0, s>>>(P_d, tiles_d);
+    launch_counter() += 1;
+}
+
+void launch_prep_f32(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, cudaStream_t s) {
+    k_prep<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, 0, nullptr);
+    launch_counter() += 1;
+}
+
+void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, double *xout,
+                     cudaStream_t s) {
+    k_prep<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, 1, xout);
+    launch_counter() += 1;
+}
+
+// One Lanczos step for every active problem of the tile table.  With
+// external_w the operator output was already written by the host path.
+void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, bool fp32_any,
+                 bool external_w, cudaStream_t s) {
+    if (!external_w) {
+        if (fp32_any) {
+            k_prep<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, 0, nullptr);
+            k_spmv_step<true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step);
+            launch_counter() += 2;
+        }
+        k_spmv_step<false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step);
+        launch_counter() += 1;
+    }
+    for (int pass = 1; pass <= 3; ++pass) {
+        k_proj<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+        k_apply<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+    }
+    launch_counter() += 6;
+}
+
+void launch_spmv(const int *row_ptr, const int *col, const double *val, int nrows, const double *x,
+                 double *y, cudaStream_t s) {
+    int blocks = (nrows + TPB - 1) / TPB;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    k_spmv_plain<double><<<blocks, TPB, 0, s>>>(row_ptr, col, val, nrows, x, y);
+    launch_counter() += 1;
+}
+
+void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, int nrows,
+                     const float *x, float *y, cudaStream_t s) {
+    int blocks = (nrows + TPB - 1) / TPB;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    k_spmv_plain<float><<<blocks, TPB, 0, s>>>(row_ptr, col, val, nrows, x, y);
+    launch_counter() += 1;
+}
+
+void launch_residuals(const int *row_ptr, const int *col, const double *val, int n, int k,
+                      const double *values_d, const double *vectors_d, int ldv, double *out4k,
+                      cudaStream_t s) {
+    int nblk = (n + TPB - 1) / TPB;
+    if (nblk > 304) nblk = 304;
+    if (nblk < 1) nblk = 1;
+    double *part = nullptr;
+    cudaMallocAsync(&part, sizeof(double) * 4 * (size_t)nblk * (size_t)k, s);
+    k_residuals<<<dim3(nblk, k), TPB, 0, s>>>(row_ptr, col, val, n, values_d, vectors_d, ldv, part);
+    k_residuals_final<<<(k + 127) / 128, 128, 0, s>>>(part, nblk, k, out4k);
+    cudaFreeAsync(part, s);
+    launch_counter() += 2;
+}
+
+}  // namespace hlanc

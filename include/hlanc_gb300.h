@@ -1,0 +1,188 @@
+/*
+ * hlanc_gb300.h -- C ABI of the GB300 (sm_103a) implicitly restarted Lanczos
+ * library.  Plain pointers, sizes and status codes; no C++ or torch types.
+ *
+ * The C++ drop-in header HLanc.hpp (same directory) sits on these entry
+ * points and keeps the reference's header-only API (namespace HLanc:
+ * dcsr_matrix_t, dcsrmv_operator_gpu, ds_solver_gpu).  Each declaration names
+ * the reference interface it replaces as HLanc.hpp:<line> of the reference
+ * header (butterfly0923/HLanc).
+ *
+ * Every entry point returns an int status (HLANC_OK == 0).  None of them
+ * exits or aborts the process; device-side waits are bounded and report
+ * HLANC_ERR_DEVICE_TIMEOUT instead of hanging.
+ */
+#ifndef HLANC_GB300_H
+#define HLANC_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define HLANC_OK                  0
+#define HLANC_NOT_CONVERGED       1  /* the reference's "return 1" (HLanc.hpp:1692,1762,1792,1806,1838,1841) */
+#define HLANC_ERR_INVALID         2  /* bad argument (ncv <= nev, ncv > n, ldv < n, ...) */
+#define HLANC_ERR_CUDA            3  /* a CUDA runtime call failed */
+#define HLANC_ERR_ALLOC           4  /* device or host allocation failed / over budget */
+#define HLANC_ERR_DEVICE_TIMEOUT  5  /* a bounded device-side wait expired */
+#define HLANC_ERR_IO              6  /* matrix file open/parse/write error */
+#define HLANC_ERR_UNSUPPORTED     7  /* size outside the supported envelope */
+#define HLANC_ERR_CALLBACK        8  /* a host operator callback reported failure */
+#define HLANC_ERR_CANCELLED       9  /* a serving request was cancelled */
+
+/* ---- precision modes --------------------------------------------------- */
+#define HLANC_PREC_FP64           0  /* FP64 SpMV (the reference's arithmetic) */
+#define HLANC_PREC_FP32_REFINE    1  /* FP32 SpMV, FP64 everywhere else, FP64 refinement */
+
+/* Largest ncv the device restart kernels accept, and largest nev. */
+#define HLANC_MAX_NCV           128
+#define HLANC_MAX_NEV            63
+
+const char *hlanc_status_string(int status);
+int hlanc_version(int *major, int *minor);   /* HLANC_VERSION_MAJOR/MINOR, HLanc.hpp:15-16 */
+
+/* ---- host CSR matrices (dcsr_matrix_t, HLanc.hpp:74-392) ---------------- */
+typedef struct hlanc_matrix_s *hlanc_matrix_t;
+
+/* dcsr_matrix_t(format, filename, is_symmetric), HLanc.hpp:103-113:
+ * format "pp" | "mm" | "bin"; parse errors return HLANC_ERR_IO. */
+int hlanc_matrix_read(const char *format, const char *filename, int is_symmetric,
+                      hlanc_matrix_t *out);
+/* In-memory construction (copies the arrays). */
+int hlanc_matrix_create(int nrows, int ncols, int nnz, const int *row_ptr, const int *col,
+                        const double *val, int is_symmetric, hlanc_matrix_t *out);
+/* get_num_rows/get_num_columns/get_nnz/symmetric, HLanc.hpp:83-89 */
+int hlanc_matrix_info(hlanc_matrix_t m, int *nrows, int *ncols, int *nnz, int *is_symmetric);
+/* get_row_ptr/get_column_index/get_value, HLanc.hpp:86-88 (borrowed pointers) */
+int hlanc_matrix_arrays(hlanc_matrix_t m, const int **row_ptr, const int **col,
+                        const double **val);
+/* save_pp/save_mm/save_bin, HLanc.hpp:287-392 */
+int hlanc_matrix_save(hlanc_matrix_t m, const char *format, const char *filename);
+int hlanc_matrix_destroy(hlanc_matrix_t m);
+
+/* ---- device CSR operator (dcsrmv_operator_gpu, HLanc.hpp:476-572) ----- */
+typedef struct hlanc_csr_s *hlanc_csr_t;
+
+/* dcsrmv_operator_gpu(m, dev), HLanc.hpp:494-514: copies the CSR to device
+ * `dev` once.  A symmetric (lower-stored) matrix is expanded to general CSR
+ * (cuSPARSE SYMMETRIC semantics, HLanc.hpp:512).  precision selects FP64
+ * values, or FP32 values for HLANC_PREC_FP32_REFINE (the FP64 copy is kept
+ * too, for refinement and residuals). */
+int hlanc_csr_create(int dev, int nrows, int ncols, int nnz, const int *row_ptr, const int *col,
+                     const double *val, int is_symmetric, int precision, hlanc_csr_t *out);
+int hlanc_csr_destroy(hlanc_csr_t op);
+int hlanc_csr_info(hlanc_csr_t op, int *dev, int *nrows, int *ncols, long long *nnz_general,
+                   int *precision);
+/* operator()(x, y), HLanc.hpp:531-572: y = A x; x and y may be host or
+ * device pointers (device pointers on the operator's device are used in
+ * place, anything else is staged).  Synchronous, like the reference. */
+int hlanc_csr_apply(hlanc_csr_t op, const double *x, double *y);
+/* y = A x on device pointers, asynchronous on `stream` (cudaStream_t). */
+int hlanc_csr_spmv_async(hlanc_csr_t op, const double *x_d, double *y_d, void *stream);
+/* FP32 SpMV (values rounded to FP32, FP32 accumulation per row). */
+int hlanc_csr_spmv_f32_async(hlanc_csr_t op, const float *x_d, float *y_d, void *stream);
+
+/* ---- solver (ds_solver_gpu, HLanc.hpp:1868-1872 / ds_solver, 1650-1850) - */
+/* Host operator callback: y = A x for host vectors of length n; return 0 on
+ * success.  This is the path for any functor that is not a device CSR
+ * operator (e.g. the reference demo's plain function, demo/HLanc_demo.cu:9-18). */
+typedef int (*hlanc_host_op_fn)(void *ctx, const double *x, double *y);
+
+typedef struct {
+    double tol;               /* <= 0: dlamch("E"), the reference's fixed tolerance (HLanc.hpp:1651) */
+    int max_restarts;         /* <= 0: 200, the reference's MAX_ITER (HLanc.hpp:1682) */
+    int precision;            /* HLANC_PREC_* (must match the operator for FP32) */
+    unsigned long long seed;  /* start-vector seed (SplitMix64 stream 0); default 0 */
+    const double *start;      /* optional host start vector of length n (overrides seed) */
+    void *stream;             /* cudaStream_t to run on; NULL = library-owned stream */
+    int use_graphs;           /* capture restart cycles as CUDA graphs (default 1 when 0 passed? see below) */
+    int reserved[7];
+} hlanc_opts_t;
+
+/* Fill defaults (tol 0, max_restarts 200, FP64, seed 0, graphs on). */
+void hlanc_opts_default(hlanc_opts_t *opts);
+
+typedef struct {
+    long long spmv_calls;     /* operator applications */
+    long long cgs_passes;     /* CGS passes incl. DGKS corrections */
+    int restarts;             /* restart cycles */
+    int nconv;                /* converged Ritz pairs */
+    int refine_restarts;      /* FP64 restart cycles after an FP32 phase */
+    int status;               /* same as the return value */
+    double rnorm;             /* final residual norm */
+    double seconds;           /* wall time of the solve */
+    double bytes_spmv;        /* algorithmic bytes moved, SpMV */
+    double bytes_cgs;         /* algorithmic bytes moved, CGS passes */
+    double bytes_restart;     /* algorithmic bytes moved, basis updates + Ritz vectors */
+    double reserved[4];
+} hlanc_stats_t;
+
+/* ds_solver_gpu(n, nev, ncv, values, vectors, ldv, op, dev): largest
+ * algebraic eigenvalues.  values (>= ncv doubles) receives the nconv
+ * converged eigenvalues ascending; vectors (host, column-major, ldv >= n,
+ * ncv columns) receives the Ritz vectors in its first nconv columns and the
+ * rest of the rotated basis after them, as the reference writes them.
+ * Exactly one of csr / host_op is used (csr takes precedence).
+ * Returns HLANC_OK, HLANC_NOT_CONVERGED (the reference's 1) or an error. */
+int hlanc_solve(int dev, int n, int nev, int ncv, double *values, double *vectors, int ldv,
+                hlanc_csr_t csr, hlanc_host_op_fn host_op, void *host_ctx,
+                const hlanc_opts_t *opts, hlanc_stats_t *stats);
+
+/* Same solve with device-resident outputs: values_d (ncv doubles) and
+ * vectors_d (ldv_d x ncv) are device pointers on `dev`.  Used when inputs and
+ * outputs stay in HBM. */
+int hlanc_solve_device(int dev, int n, int nev, int ncv, double *values_d, double *vectors_d,
+                       int ldv_d, hlanc_csr_t csr, const hlanc_opts_t *opts,
+                       hlanc_stats_t *stats);
+
+/* ---- residual verifier (demo/verify_eigs.cu:52-98) ---------------------- */
+/* For k pairs (values[i], vectors[:, i]) on the device, computes
+ * resid[i] = ||A v_i - lambda_i v_i||_2 and rdiff[i] = max_r |(Av)_r - (lambda v)_r| /
+ * max(max|Av|, max|lambda v|) (verify_eigs' rdiff).  Device pointers; synchronous. */
+int hlanc_residuals_device(hlanc_csr_t csr, int k, const double *values_d,
+                           const double *vectors_d, int ldv_d, double *resid_h, double *rdiff_h);
+
+/* ---- batched solves (one launch sequence over many problems) ----------- */
+typedef struct hlanc_batch_s *hlanc_batch_t;
+
+int hlanc_batch_create(int dev, int nprob, const hlanc_csr_t *ops, const int *nev,
+                       const int *ncv, const hlanc_opts_t *opts, hlanc_batch_t *out);
+/* Runs every problem to completion.  values_d[i] / vectors_d[i] are device
+ * outputs (ncv[i] doubles, n_i x ncv[i] with ld n_i); status[i] per problem. */
+int hlanc_batch_run(hlanc_batch_t b, double **values_d, double **vectors_d, int *status,
+                    hlanc_stats_t *stats);
+int hlanc_batch_destroy(hlanc_batch_t b);
+
+/* ---- serving: continuous batching of solves ----------------------------- */
+typedef struct hlanc_server_s *hlanc_server_t;
+
+typedef struct {
+    size_t mem_budget_bytes;  /* admission budget: CSR + basis + workspace */
+    int max_slots;            /* problems resident at once */
+    int dev;
+} hlanc_server_opts_t;
+
+int hlanc_server_create(const hlanc_server_opts_t *opts, hlanc_server_t *out);
+/* Submit a solve on an existing device operator; returns a request id. */
+int hlanc_server_submit(hlanc_server_t s, hlanc_csr_t csr, int nev, int ncv,
+                        const hlanc_opts_t *opts, long long *request_id);
+/* Advance the scheduler by one restart-cycle tick (admits, runs, retires). */
+int hlanc_server_step(hlanc_server_t s, int *active, int *pending);
+/* Poll a request: *done = 1 when finished; then values (ncv) / vectors (n x ncv,
+ * ld n, host) are filled and *status is its solve status. */
+int hlanc_server_poll(hlanc_server_t s, long long request_id, int *done, int *status,
+                      double *values, double *vectors, hlanc_stats_t *stats);
+int hlanc_server_cancel(hlanc_server_t s, long long request_id);
+int hlanc_server_destroy(hlanc_server_t s);
+
+/* ---- diagnostics ---------------------------------------------------------- */
+/* Number of kernels this library launched since load (all devices). */
+long long hlanc_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

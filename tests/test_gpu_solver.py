@@ -1,0 +1,224 @@
+"""GPU parity of ds_solver_gpu / dcsrmv_operator_gpu against the reference's
+own CPU solver (golden fixtures from ds_solver_mkl), the oracle, and analytic
+spectra.  Tolerances (FP64 mode): eigenvalues within 1e-10 relative of the
+reference, residuals ||A v - lambda v|| <= 1e-10 ||A||, eigenvectors equal up
+to sign (|<v, v_ref>| within 1e-8 of 1) where the eigenvalue is simple."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from hlanc_gb300 import generators as G
+
+pytestmark = pytest.mark.gpu
+
+EV_RTOL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def H():
+    import hlanc_gb300 as H
+    from hlanc_gb300 import build
+    build.build()
+    return H
+
+
+def _norm_a(m):
+    return float(np.abs(G.to_scipy(m)).sum(axis=1).max())
+
+
+def _check_pairs(m, vals, vecs, k, tol=1e-10):
+    A = G.to_scipy(m)
+    V = vecs[: m.n, :k]
+    R = A @ V - V * vals[:k]
+    assert np.linalg.norm(R, axis=0).max() <= tol * _norm_a(m)
+    assert np.abs(V.T @ V - np.eye(k)).max() < 1e-10
+    assert np.all(np.diff(vals[:k]) >= 0)
+
+
+@pytest.mark.parametrize("case,gen,nev,ncv", [
+    ("c1_laplacian2d_100", lambda: G.laplacian_2d(100), 10, 30),
+    ("lap3d_12_shift", lambda: G.laplacian_3d(12, shift_seed=1), 20, 60),
+    ("banded_3000_bw5", lambda: G.banded_random(3000, 5, seed=3, problem=0), 8, 24),
+    ("chunglu_4096", lambda: G.chung_lu_normalized(4096, seed=2), 16, 48),
+])
+def test_eigenvalues_match_reference(H, case, gen, nev, ncv):
+    g = golden(f"{case}.npz")
+    m = gen()
+    op = H.dcsrmv_operator_gpu(m)
+    rc, vals, vecs, st = H.solve(op, nev, ncv, seed=int(g["seed"]))
+    assert rc == 0, st
+    assert st["nconv"] >= nev
+    ref = g["values"]
+    assert np.abs(vals[:nev] - ref).max() <= EV_RTOL * np.abs(ref).max()
+    _check_pairs(m, vals, vecs, nev)
+
+
+def test_c1_analytic(H):
+    m = G.laplacian_2d(100)
+    op = H.dcsrmv_operator_gpu(m)
+    rc, vals, vecs, st = H.solve(op, 10, 30)
+    assert rc == 0
+    ana = G.laplacian_2d_eigenvalues(100)[-10:]
+    assert np.abs(vals[:10] - ana).max() < 1e-12
+    _check_pairs(m, vals, vecs, 10)
+
+
+@pytest.mark.parametrize("case,sym", [("simple_pp", False), ("journals_mtx", True)])
+def test_demo_matrices_with_vectors(H, readers_golden, case, sym):
+    tag = "simple" if case == "simple_pp" else "journals"
+    g = golden(f"{case}.npz")
+    mat = H.dcsr_matrix_t.from_arrays(readers_golden[f"{tag}_row_ptr"], readers_golden[f"{tag}_col"],
+                                      readers_golden[f"{tag}_val"], int(readers_golden[f"{tag}_meta"][1]), sym)
+    n = mat.get_num_rows()
+    op = H.dcsrmv_operator_gpu(mat)
+    values = np.zeros(12)
+    vectors = np.zeros((n, 12), order="F")
+    rc = H.ds_solver_gpu(n, 4, 12, values, vectors, n, op)
+    assert rc == 0
+    ref = g["values"]
+    assert np.abs(values[:4] - ref).max() <= EV_RTOL * np.abs(ref).max()
+    dots = np.abs(np.sum(vectors[:, :4] * g["vectors"], axis=0))
+    assert np.all(np.abs(dots - 1.0) < 1e-8)
+
+
+def test_function_operator(H):
+    # a plain callable as the operator (demo/HLanc_demo.cu:9-18,164)
+    K = G.simple_dense(16)
+
+    def op_fun_simple(x, y):
+        y[:] = K @ x
+
+    values = np.zeros(12)
+    vectors = np.zeros((16, 12), order="F")
+    rc = H.ds_solver_gpu(16, 4, 12, values, vectors, 16, op_fun_simple)
+    assert rc == 0
+    ref = golden("simple_pp.npz")["values"]
+    assert np.abs(values[:4] - ref).max() <= EV_RTOL * np.abs(ref).max()
+    R = K @ vectors[:, :4] - vectors[:, :4] * values[:4]
+    assert np.linalg.norm(R, axis=0).max() < 1e-10 * np.abs(K).sum(axis=1).max()
+
+
+def test_vectors_odd_grid_and_ldv(H):
+    g = golden("lap2d_odd_37x23.npz")
+    m = G.laplacian_2d(37, 23)
+    op = H.dcsrmv_operator_gpu(m)
+    ldv = m.n + 7
+    values = np.zeros(20)
+    vectors = np.zeros((ldv, 20), order="F")
+    vectors[m.n:, :] = 12345.0
+    o = H.opts(seed=5)
+    rc = H.ds_solver_gpu(m.n, 6, 20, values, vectors, ldv, op, opts_=o)
+    assert rc == 0
+    assert np.abs(values[:6] - g["values"]).max() < 1e-12 * 8
+    dots = np.abs(np.sum(vectors[: m.n, :6] * g["vectors"], axis=0))
+    assert np.all(np.abs(dots - 1.0) < 1e-8)
+    assert np.all(vectors[m.n:, :] == 12345.0)          # padding rows untouched
+
+
+def test_matches_oracle_on_same_start(H, oracle_mod):
+    m = G.banded_random(1500, 3, seed=11, problem=4)
+    x0 = G.start_vector(m.n, 9)
+    rc_o, vals_o, vecs_o, _ = oracle_mod.solve_csr(m.row_ptr, m.col, m.val, m.ncols, False, 6, 18, x0)
+    op = H.dcsrmv_operator_gpu(m)
+    rc, vals, vecs, st = H.solve(op, 6, 18, start=x0)
+    assert rc == rc_o == 0
+    assert np.abs(vals[:6] - vals_o[:6]).max() <= EV_RTOL * np.abs(vals_o[:6]).max()
+
+
+def test_spmv_operator_host_and_device(H, readers_golden):
+    import torch
+    s = golden("spmv.npz")
+    g = readers_golden
+    mat = H.dcsr_matrix_t.from_arrays(g["journals_row_ptr"], g["journals_col"], g["journals_val"],
+                                      int(g["journals_meta"][1]), True)
+    op = H.dcsrmv_operator_gpu(mat)
+    y = np.zeros(op.n)
+    op(np.ascontiguousarray(s["x_sym"]), y)
+    assert np.allclose(y, s["y_sym_mkl"], rtol=1e-13, atol=1e-9)
+    xd = torch.from_numpy(s["x_sym"]).cuda()
+    yd = torch.zeros_like(xd)
+    op(xd, yd)
+    torch.cuda.synchronize()
+    assert np.allclose(yd.cpu().numpy(), s["y_sym_mkl"], rtol=1e-13, atol=1e-9)
+    lap = G.laplacian_2d(7, 5)
+    op2 = H.dcsrmv_operator_gpu(lap)
+    y2 = np.zeros(lap.n)
+    op2(np.ascontiguousarray(s["x_gen"]), y2)
+    assert np.allclose(y2, s["y_gen"], rtol=1e-14, atol=1e-14)
+
+
+def test_spmv_long_rows_and_empty_rows(H, oracle_mod):
+    # power-law rows (> 96 entries use the warp path) and empty rows
+    rng = np.random.default_rng(5)
+    n = 3000
+    lens = np.minimum(rng.zipf(1.6, n), 2000)
+    lens[::17] = 0
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    ci = rng.integers(0, n, rp[-1]).astype(np.int32)
+    va = rng.standard_normal(rp[-1])
+    m = G.CSR(n, n, rp, ci, va)
+    op = H.dcsrmv_operator_gpu(m)
+    x = rng.standard_normal(n)
+    y = np.zeros(n)
+    op(x, y)
+    ref = oracle_mod.spmv(rp, ci, va, n, False, x, kind="naive")
+    assert np.allclose(y, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_mixed_precision_refined(H):
+    g = golden("chunglu_4096.npz")
+    m = G.chung_lu_normalized(4096, seed=2)
+    op = H.dcsrmv_operator_gpu(m, precision=H.HLANC_PREC_FP32_REFINE)
+    rc, vals, vecs, st = H.solve(op, 16, 48, precision=H.HLANC_PREC_FP32_REFINE, seed=int(g["seed"]))
+    assert rc == 0, st
+    ref = g["values"]
+    assert np.abs(vals[:16] - ref).max() <= EV_RTOL * np.abs(ref).max()
+    _check_pairs(m, vals, vecs, 16)
+
+
+def test_tolerance_option(H):
+    m = G.laplacian_3d(16, shift_seed=1)
+    op = H.dcsrmv_operator_gpu(m)
+    rc, vals, vecs, st = H.solve(op, 20, 60, tol=1e-10)
+    assert rc == 0
+    _check_pairs(m, vals, vecs, 20, tol=1e-9)
+    rc2, vals2, _, st2 = H.solve(op, 20, 60)
+    assert rc2 == 0
+    assert st["spmv_calls"] <= st2["spmv_calls"]
+    assert np.abs(vals[:20] - vals2[:20]).max() < 1e-10 * 12
+
+
+def test_not_converged_returns_1(H):
+    m = G.laplacian_2d(60)
+    op = H.dcsrmv_operator_gpu(m)
+    values = np.zeros(30)
+    vectors = np.zeros((m.n, 30), order="F")
+    rc = H.ds_solver_gpu(m.n, 10, 30, values, vectors, m.n, op, opts_=H.opts(max_restarts=1))
+    assert rc == 1
+    assert np.all(values == 0)
+
+
+def test_invalid_arguments(H):
+    m = G.laplacian_2d(8)
+    op = H.dcsrmv_operator_gpu(m)
+    for nev, ncv in ((4, 4), (3, 65), (0, 4)):
+        with pytest.raises(H.HLancError):
+            H.ds_solver_gpu(m.n, nev, ncv, np.zeros(70), np.zeros((m.n, 70), order="F"), m.n, op)
+
+
+def test_graph_and_eager_agree(H):
+    m = G.laplacian_2d(50)
+    op = H.dcsrmv_operator_gpu(m)
+    rc1, v1, _, s1 = H.solve(op, 8, 24, use_graphs=True)
+    rc2, v2, _, s2 = H.solve(op, 8, 24, use_graphs=False)
+    assert rc1 == rc2 == 0
+    assert np.array_equal(v1, v2)                  # same kernels, same order: bit-identical
+    assert s1["spmv_calls"] == s2["spmv_calls"]
+
+
+def test_native_library_loaded(H):
+    import os
+    with open("/proc/self/maps") as f:
+        maps = f.read()
+    assert os.path.basename(H.LIB_PATH) in maps
+    assert H.kernel_launches() > 0
