@@ -42,7 +42,8 @@ class HLancError(RuntimeError):
 class Opts(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_restarts", C.c_int), ("precision", C.c_int),
                 ("seed", C.c_ulonglong), ("start", C.POINTER(C.c_double)), ("stream", C.c_void_p),
-                ("use_graphs", C.c_int), ("reserved", C.c_int * 7)]
+                ("use_graphs", C.c_int), ("restart_on_device", C.c_int), ("profile", C.c_int),
+                ("reserved", C.c_int * 5)]
 
 
 class Stats(C.Structure):
@@ -53,6 +54,22 @@ class Stats(C.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+PROF_CLASSES = ("spmv", "cgs_proj", "cgs_apply", "basis", "ritz", "aux", "host_restart")
+
+
+class Profile(C.Structure):
+    _fields_ = [("launches", C.c_longlong * 7), ("ms", C.c_double * 7), ("bytes", C.c_double * 7),
+                ("flops", C.c_double * 7)]
+
+    def as_dict(self) -> dict:
+        return {name: dict(launches=self.launches[i], ms=self.ms[i], bytes=self.bytes[i], flops=self.flops[i])
+                for i, name in enumerate(PROF_CLASSES)}
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("mem_budget_bytes", C.c_size_t), ("max_slots", C.c_int), ("dev", C.c_int)]
 
 
 HOST_OP = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double))
@@ -85,6 +102,16 @@ def _declare(L):
                              C.POINTER(Stats)]),
         "hlanc_solve_device": (_i, [_i, _i, _i, _i, _p, _p, _i, _p, C.POINTER(Opts), C.POINTER(Stats)]),
         "hlanc_residuals_device": (_i, [_p, _i, _p, _p, _i, _p, _p]),
+        "hlanc_last_profile": (_i, [C.POINTER(Profile)]),
+        "hlanc_batch_create": (_i, [_i, _i, _p, _p, _p, C.POINTER(Opts), C.POINTER(_p)]),
+        "hlanc_batch_run": (_i, [_p, _p, _p, _p, C.POINTER(Stats)]),
+        "hlanc_batch_destroy": (_i, [_p]),
+        "hlanc_server_create": (_i, [C.POINTER(ServerOpts), C.POINTER(_p)]),
+        "hlanc_server_submit": (_i, [_p, _p, _i, _i, C.POINTER(Opts), C.POINTER(C.c_longlong)]),
+        "hlanc_server_step": (_i, [_p, _ip, _ip]),
+        "hlanc_server_poll": (_i, [_p, C.c_longlong, _ip, _ip, _p, _p, C.POINTER(Stats)]),
+        "hlanc_server_cancel": (_i, [_p, C.c_longlong]),
+        "hlanc_server_destroy": (_i, [_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -109,11 +136,14 @@ def _check(rc: int, what: str) -> None:
 
 
 def opts(tol: float = 0.0, max_restarts: int = 200, precision: int = HLANC_PREC_FP64, seed: int = 0,
-         start: Optional[np.ndarray] = None, stream: int = 0, use_graphs: bool = True):
+         start: Optional[np.ndarray] = None, stream: int = 0, use_graphs: bool = True,
+         restart_on_device: bool = False, profile: bool = False):
     o = Opts()
     lib().hlanc_opts_default(C.byref(o))
     o.tol, o.max_restarts, o.precision, o.seed = tol, max_restarts, precision, seed
     o.use_graphs = int(use_graphs)
+    o.restart_on_device = int(restart_on_device)
+    o.profile = int(profile)
     o.stream = stream or None
     keep = None
     if start is not None:
@@ -319,3 +349,98 @@ def residuals_device(op: dcsrmv_operator_gpu, k: int, values_ptr: int, vectors_p
 
 def kernel_launches() -> int:
     return int(lib().hlanc_kernel_launches())
+
+
+def last_profile() -> dict:
+    """Per-kernel-class timing of the last solve run with profile=True."""
+    p = Profile()
+    _check(lib().hlanc_last_profile(C.byref(p)), "last_profile")
+    return p.as_dict()
+
+
+# ---- batched solves ------------------------------------------------------------------
+class Batch:
+    """Many independent solves advanced by one launch sequence per restart
+    cycle (hlanc_batch_*).  Outputs are device buffers (torch tensors)."""
+
+    def __init__(self, ops, nev, ncv, dev: int = 0, **kw):
+        self.ops = list(ops)
+        k = len(self.ops)
+        self.nev = np.ascontiguousarray(np.broadcast_to(np.asarray(nev, dtype=np.int32), (k,)))
+        self.ncv = np.ascontiguousarray(np.broadcast_to(np.asarray(ncv, dtype=np.int32), (k,)))
+        self._o, self._keep = opts(**kw)
+        handles = (C.c_void_p * k)(*[o.handle.value if hasattr(o.handle, "value") else o.handle for o in self.ops])
+        h = C.c_void_p()
+        _check(lib().hlanc_batch_create(dev, k, handles, self.nev.ctypes.data, self.ncv.ctypes.data,
+                                        C.byref(self._o), C.byref(h)), "hlanc_batch_create")
+        self._h, self.dev = h, dev
+
+    def run(self, values_ptrs, vectors_ptrs):
+        k = len(self.ops)
+        vp = (C.c_void_p * k)(*values_ptrs)
+        xp = (C.c_void_p * k)(*vectors_ptrs)
+        status = np.zeros(k, dtype=np.int32)
+        st = Stats()
+        rc = lib().hlanc_batch_run(self._h, vp, xp, status.ctypes.data, C.byref(st))
+        if rc not in (HLANC_OK, HLANC_NOT_CONVERGED):
+            raise HLancError(rc, "hlanc_batch_run")
+        d = st.as_dict()
+        d["rc"] = rc
+        return status, d
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.hlanc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+# ---- serving ---------------------------------------------------------------------------
+class Server:
+    """Continuous batching of eigen-solves (hlanc_server_*): requests are
+    admitted by slot count and device-memory budget, every resident solve
+    advances one restart cycle per step(), finished solves are retired."""
+
+    def __init__(self, mem_budget_bytes: int, max_slots: int, dev: int = 0):
+        so = ServerOpts(mem_budget_bytes, max_slots, dev)
+        h = C.c_void_p()
+        _check(lib().hlanc_server_create(C.byref(so), C.byref(h)), "hlanc_server_create")
+        self._h, self.dev = h, dev
+        self._req = {}
+
+    def submit(self, op: dcsrmv_operator_gpu, nev: int, ncv: int, **kw) -> int:
+        o, keep = opts(**kw)
+        rid = C.c_longlong()
+        _check(lib().hlanc_server_submit(self._h, op.handle, nev, ncv, C.byref(o), C.byref(rid)), "submit")
+        self._req[rid.value] = (op.n, nev, ncv)
+        return rid.value
+
+    def step(self):
+        a, p = _i(), _i()
+        _check(lib().hlanc_server_step(self._h, C.byref(a), C.byref(p)), "hlanc_server_step")
+        return a.value, p.value
+
+    def poll(self, rid: int):
+        n, nev, ncv = self._req[rid]
+        done, status = _i(), _i()
+        values = np.zeros(ncv)
+        vectors = np.zeros((n, ncv), order="F")
+        st = Stats()
+        _check(lib().hlanc_server_poll(self._h, rid, C.byref(done), C.byref(status), values.ctypes.data,
+                                       vectors.ctypes.data, C.byref(st)), "poll")
+        if not done.value:
+            return None
+        return status.value, values, vectors, st.as_dict()
+
+    def cancel(self, rid: int) -> None:
+        _check(lib().hlanc_server_cancel(self._h, rid), "cancel")
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.hlanc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

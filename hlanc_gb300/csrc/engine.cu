@@ -25,6 +25,7 @@
 
 #include "../../include/HLanc.hpp"
 #include "internal.cuh"
+#include "restart_host.h"
 
 using namespace hlanc;
 
@@ -64,6 +65,48 @@ struct hlanc_matrix_s {
     HLanc::dcsr_matrix_t m;
 };
 
+namespace hlanc {
+
+// ---- launch profiler ---------------------------------------------------------
+struct Profiler {
+    std::vector<cudaEvent_t> pool;
+    size_t next = 0;
+    struct Rec { int cls; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    cudaEvent_t pending = nullptr;
+    double host_ms = 0.0;
+    long long host_n = 0;
+    cudaEvent_t get() {
+        if (next == pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+        }
+        return pool[next++];
+    }
+    ~Profiler() {
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+static thread_local Profiler *g_prof = nullptr;
+static thread_local hlanc_profile_t g_last_prof;
+static thread_local bool g_have_prof = false;
+
+void prof_begin(cudaStream_t s) {
+    if (!g_prof) return;
+    g_prof->pending = g_prof->get();
+    cudaEventRecord(g_prof->pending, s);
+}
+void prof_end(int cls, cudaStream_t s) {
+    if (!g_prof || !g_prof->pending) return;
+    cudaEvent_t b = g_prof->get();
+    cudaEventRecord(b, s);
+    g_prof->recs.push_back({cls, g_prof->pending, b});
+    g_prof->pending = nullptr;
+}
+
+}  // namespace hlanc
+
 namespace {
 
 struct DevGuard {
@@ -79,23 +122,29 @@ struct DevGuard {
     }
 };
 
+// Rows per tile: about 4 tiles per SM for large problems (152 SMs), at
+// least 128 rows, a multiple of 64.
 int tile_rows_for(int n) {
-    long long tr = ((long long)n + 1215) / 1216;         // ~1216 tiles per large problem
+    long long tr = ((long long)n + 607) / 608;
     tr = (tr + ROW_ALIGN - 1) / ROW_ALIGN * ROW_ALIGN;
     if (tr < 128) tr = 128;
-    if (tr > 8192) tr = 8192;
+    if (tr > (1 << 16)) tr = 1 << 16;
     return (int)tr;
 }
 
-// ---- one problem's device resources ---------------------------------------------
+constexpr int MBOX_STATE = 32;   // doubles reserved for State in a mailbox slot
+
+long long mbox_slot(int m) { return MBOX_STATE + 2LL * m + (long long)m * m + m; }
+
+// ---- one problem's device resources and host mirror --------------------------------
 struct ProbRes {
-    int n = 0, ncv = 0, nev0 = 0, ld = 0, ntiles = 0, tr = 0, pstride = 0;
+    int n = 0, ncv = 0, nev0 = 0, ld = 0, ntiles = 0, tr = 0, pstride = 0, ngroups = 0;
     int fp32 = 0;
     hlanc_csr_s *csr = nullptr;
     hlanc_host_op_fn host_op = nullptr;
     void *host_ctx = nullptr;
-    double *block = nullptr;       // V | r0 | r1 | part | small
-    double *V = nullptr, *r0 = nullptr, *r1 = nullptr, *part = nullptr, *small = nullptr;
+    double *block = nullptr;   // V | r0 | r1 | part | gpart | small
+    double *V = nullptr, *r0 = nullptr, *r1 = nullptr, *part = nullptr, *gpart = nullptr, *small = nullptr;
     State *st = nullptr;
     unsigned *counter = nullptr;
     float *x32 = nullptr;
@@ -103,16 +152,21 @@ struct ProbRes {
     int ldo = 0;
     bool own_vout = false;
     size_t bytes = 0;
+    int cycles = 0;            // restart cycles launched
+    bool live = false;         // resources allocated
+    // host mirror (host restart)
+    std::vector<double> h, ritz_s, bnds_s, Q, values;
+    State hs;
 
     static size_t estimate(int n, int ncv, int fp32) {
-        const int ld = (n + ROW_ALIGN - 1) / ROW_ALIGN * ROW_ALIGN;
+        const size_t ld = ((size_t)n + ROW_ALIGN - 1) / ROW_ALIGN * ROW_ALIGN;
         const int tr = tile_rows_for(n);
-        const int ntiles = (n + tr - 1) / tr;
-        const int pst = (ncv + 2 + 1) & ~1;
-        size_t d = (size_t)ld * ncv + 2 * (size_t)ld + (size_t)ntiles * pst + SM_SIZE(ncv);
-        size_t b = d * sizeof(double) + sizeof(State) + 256;
-        if (fp32) b += (size_t)ld * sizeof(float);
-        b += (size_t)ld * ncv * sizeof(double);   // Ritz output
+        const size_t nt = ((size_t)n + tr - 1) / tr, ng = (nt + RGROUP - 1) / RGROUP;
+        const size_t pst = (size_t)((ncv + 2 + 1) & ~1);
+        size_t d = ld * ncv + 2 * ld + (nt + ng) * pst + SM_SIZE(ncv);
+        size_t b = d * sizeof(double) + 1024 + 4 * ng;
+        if (fp32) b += ld * sizeof(float);
+        b += ld * ncv * sizeof(double);   // Ritz output
         return b;
     }
 
@@ -120,26 +174,36 @@ struct ProbRes {
         ld = (n + ROW_ALIGN - 1) / ROW_ALIGN * ROW_ALIGN;
         tr = tile_rows_for(n);
         ntiles = (n + tr - 1) / tr;
+        ngroups = (ntiles + RGROUP - 1) / RGROUP;
         pstride = (ncv + 2 + 1) & ~1;
-        const size_t nd = (size_t)ld * ncv + 2 * (size_t)ld + (size_t)ntiles * pstride + SM_SIZE(ncv);
+        const size_t nd = (size_t)ld * ncv + 2 * (size_t)ld + (size_t)(ntiles + ngroups) * pstride + SM_SIZE(ncv);
         bytes = nd * sizeof(double);
         CK(cudaMalloc(&block, bytes));
+        live = true;
         CK(cudaMemsetAsync(block, 0, bytes, s));
         V = block;
         r0 = V + (size_t)ld * ncv;
         r1 = r0 + ld;
         part = r1 + ld;
-        small = part + (size_t)ntiles * pstride;
+        gpart = part + (size_t)ntiles * pstride;
+        small = gpart + (size_t)ngroups * pstride;
+        const size_t sb = 512 + 4 * ((size_t)ngroups + 1);
         void *sp = nullptr;
-        CK(cudaMalloc(&sp, sizeof(State) + 256));
-        CK(cudaMemsetAsync(sp, 0, sizeof(State) + 256, s));
+        CK(cudaMalloc(&sp, sb));
+        CK(cudaMemsetAsync(sp, 0, sb, s));
         st = (State *)sp;
-        counter = (unsigned *)((char *)sp + sizeof(State) + 64);
+        counter = (unsigned *)((char *)sp + 512);
+        bytes += sb;
         if (fp32) {
             CK(cudaMalloc(&x32, (size_t)ld * sizeof(float)));
             CK(cudaMemsetAsync(x32, 0, (size_t)ld * sizeof(float), s));
             bytes += (size_t)ld * sizeof(float);
         }
+        h.assign(2 * ncv, 0.0);
+        ritz_s.assign(ncv, 0.0);
+        bnds_s.assign(ncv, 0.0);
+        Q.assign((size_t)ncv * ncv, 0.0);
+        values.assign(ncv, 0.0);
         return HLANC_OK;
     }
     void release() {
@@ -147,7 +211,8 @@ struct ProbRes {
         if (st) cudaFree(st);
         if (x32) cudaFree(x32);
         if (own_vout && vout) cudaFree(vout);
-        block = nullptr; st = nullptr; x32 = nullptr; vout = nullptr;
+        block = nullptr; st = nullptr; x32 = nullptr; vout = nullptr; own_vout = false;
+        live = false;
     }
 };
 
@@ -177,17 +242,24 @@ public:
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     bool use_graphs = true;
+    bool device_restart = false;
     std::vector<ProbRes> probs;
-    std::vector<int> active;            // indices of problems in the launch tables
+    std::vector<int> active;             // problems in the launch tables, in slot order
     Problem *P_d = nullptr;
     Tile *T_d = nullptr;
-    int ntiles = 0, nslots = 0;
-    State *st_h = nullptr;              // pinned mirror of every problem's State
-    int st_cap = 0;
-    int max_ncv = 0, max_nev0 = 0;
+    int ntiles = 0, nslots_cap = 0, ntiles_cap = 0;
+    int max_ncv = 0;
     bool fp32_any = false;
     std::map<long long, cudaGraphExec_t> graphs;
-    double *xs_h = nullptr, *ys_h = nullptr, *xs_d = nullptr;   // host-operator staging
+    // host-restart mailbox
+    std::vector<long long> off_h;
+    long long *off_d = nullptr;
+    int *flag_d = nullptr, *flag_h = nullptr;
+    double *mbox_d = nullptr, *mbox_h = nullptr;
+    long long mbox_used = 0, mbox_cap = 0;
+    int flags_cap = 0;
+    // host-operator staging
+    double *xs_h = nullptr, *ys_h = nullptr, *xs_d = nullptr;
     size_t xs_cap = 0;
 
     ~Engine() {
@@ -196,16 +268,21 @@ public:
         for (auto &p : probs) p.release();
         if (P_d) cudaFree(P_d);
         if (T_d) cudaFree(T_d);
-        if (st_h) cudaFreeHost(st_h);
+        if (off_d) cudaFree(off_d);
+        if (flag_d) cudaFree(flag_d);
+        if (mbox_d) cudaFree(mbox_d);
+        if (mbox_h) cudaFreeHost(mbox_h);
+        if (flag_h) cudaFreeHost(flag_h);
         if (xs_h) cudaFreeHost(xs_h);
         if (ys_h) cudaFreeHost(ys_h);
         if (xs_d) cudaFree(xs_d);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 
-    int init(int device, void *user_stream, bool graphs_on) {
+    int init(int device, void *user_stream, bool graphs_on, bool dev_restart) {
         dev = device;
         use_graphs = graphs_on;
+        device_restart = dev_restart;
         if (user_stream) {
             stream = (cudaStream_t)user_stream;
         } else {
@@ -220,25 +297,29 @@ public:
         graphs.clear();
     }
 
-    int add(int n, int nev, int ncv, hlanc_csr_s *csr, hlanc_host_op_fn host_op, void *host_ctx,
-            int fp32, const hlanc_opts_t &o, int *index) {
+    int add(int n, int nev, int ncv, hlanc_csr_s *csr, hlanc_host_op_fn host_op, void *host_ctx, int fp32,
+            const hlanc_opts_t &o, int *index) {
         ProbRes p;
         p.n = n; p.ncv = ncv; p.nev0 = nev; p.csr = csr; p.host_op = host_op; p.host_ctx = host_ctx;
         p.fp32 = fp32;
         int rc = p.alloc(stream);
         if (rc) { p.release(); return rc == HLANC_ERR_CUDA ? HLANC_ERR_ALLOC : rc; }
         State S = initial_state(nev, ncv, o);
+        p.hs = S;
         CK(cudaMemcpyAsync(p.st, &S, sizeof S, cudaMemcpyHostToDevice, stream));
-        probs.push_back(p);
+        probs.push_back(std::move(p));
         *index = (int)probs.size() - 1;
         return HLANC_OK;
     }
 
-    // Rebuild the device descriptor and tile tables for the problems in `active`.
+    // Rebuild the descriptor/tile tables and the mailbox layout for `active`.
     int upload() {
         std::vector<Problem> P(active.size());
         std::vector<Tile> T;
-        max_ncv = 0; max_nev0 = 0; fp32_any = false;
+        max_ncv = 0;
+        fp32_any = false;
+        off_h.assign(active.size(), 0);
+        long long off = 0;
         for (size_t a = 0; a < active.size(); ++a) {
             ProbRes &p = probs[active[a]];
             Problem &q = P[a];
@@ -251,7 +332,7 @@ public:
             q.n = p.n; q.ld = p.ld; q.ncv = p.ncv; q.nev0 = p.nev0;
             q.tile0 = (int)T.size(); q.ntiles = p.ntiles;
             q.fp32 = p.fp32; q.pstride = p.pstride;
-            q.V = p.V; q.r0 = p.r0; q.r1 = p.r1; q.part = p.part; q.counter = p.counter;
+            q.V = p.V; q.r0 = p.r0; q.r1 = p.r1; q.part = p.part; q.gpart = p.gpart; q.counter = p.counter;
             q.st = p.st; q.small = p.small;
             q.wext = p.csr ? nullptr : p.r0;     // non-null marks the host-operator path
             q.vout = p.vout; q.ldo = p.ldo;
@@ -264,24 +345,42 @@ public:
                 T.push_back(tl);
             }
             max_ncv = std::max(max_ncv, p.ncv);
-            max_nev0 = std::max(max_nev0, p.nev0);
             fp32_any = fp32_any || p.fp32;
+            off_h[a] = off;
+            off += mbox_slot(p.ncv);
         }
-        if ((int)active.size() > nslots || (int)T.size() > ntiles || !P_d || !T_d) {
+        mbox_used = off;
+        const int na = std::max<int>((int)active.size(), 1);
+        if (na > nslots_cap) {
             if (P_d) cudaFree(P_d);
+            if (off_d) cudaFree(off_d);
+            if (flag_d) cudaFree(flag_d);
+            if (flag_h) cudaFreeHost(flag_h);
+            nslots_cap = na + 8;
+            CK(cudaMalloc(&P_d, sizeof(Problem) * nslots_cap));
+            CK(cudaMalloc(&off_d, sizeof(long long) * nslots_cap));
+            CK(cudaMalloc(&flag_d, sizeof(int) * nslots_cap));
+            CK(cudaMallocHost(&flag_h, sizeof(int) * nslots_cap));
+        }
+        if ((int)T.size() > ntiles_cap || !T_d) {
             if (T_d) cudaFree(T_d);
-            nslots = std::max<int>((int)active.size(), 1);
-            CK(cudaMalloc(&P_d, sizeof(Problem) * nslots));
-            CK(cudaMalloc(&T_d, sizeof(Tile) * std::max<size_t>(T.size(), 1)));
+            ntiles_cap = std::max<int>((int)T.size(), 1) + 64;
+            CK(cudaMalloc(&T_d, sizeof(Tile) * ntiles_cap));
+        }
+        if (mbox_used > mbox_cap) {
+            if (mbox_d) cudaFree(mbox_d);
+            if (mbox_h) cudaFreeHost(mbox_h);
+            mbox_cap = mbox_used + 4096;
+            CK(cudaMalloc(&mbox_d, sizeof(double) * mbox_cap));
+            CK(cudaMallocHost(&mbox_h, sizeof(double) * mbox_cap));
         }
         ntiles = (int)T.size();
         if (!P.empty()) CK(cudaMemcpyAsync(P_d, P.data(), sizeof(Problem) * P.size(), cudaMemcpyHostToDevice, stream));
         if (!T.empty()) CK(cudaMemcpyAsync(T_d, T.data(), sizeof(Tile) * T.size(), cudaMemcpyHostToDevice, stream));
-        if ((int)active.size() > st_cap) {
-            if (st_h) cudaFreeHost(st_h);
-            st_cap = (int)active.size() + 8;
-            CK(cudaMallocHost(&st_h, sizeof(State) * st_cap));
-        }
+        if (!active.empty())
+            CK(cudaMemcpyAsync(off_d, off_h.data(), sizeof(long long) * active.size(), cudaMemcpyHostToDevice, stream));
+        for (size_t a = 0; a < active.size(); ++a) flag_h[a] = 0;
+        CK(cudaStreamSynchronize(stream));   // off_h / flag_h are reused by later async copies
         drop_graphs();
         return HLANC_OK;
     }
@@ -296,49 +395,85 @@ public:
         ProbRes &p = probs[prob];
         if (o.start) {
             CK(cudaMemcpyAsync(p.r0, o.start, sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
+            CK(cudaStreamSynchronize(stream));   // o.start may be pageable / short-lived
         } else {
             launch_start_vector(P_d, T_d, ntiles, slot_of(prob), o.seed, stream);
         }
-        launch_norm_init(P_d, T_d, ntiles, stream);
         return HLANC_OK;
     }
 
-    int readback() {
-        for (size_t a = 0; a < active.size(); ++a)
-            CK(cudaMemcpyAsync(st_h + a, probs[active[a]].st, sizeof(State), cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
+    int norm_init() {
+        launch_norm_init(P_d, T_d, ntiles, stream);
         CK(cudaGetLastError());
         return HLANC_OK;
     }
 
-    void enqueue_cycle(int steps, int basis_nev) {
-        if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_nev, stream);
-        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, s, fp32_any, false, stream);
-        launch_restart(P_d, (int)active.size(), max_ncv, stream);
+    static int basis_bucket(int nev) {
+        if (nev <= 0) return 0;
+        const int b[] = {8, 16, 24, 32, 48, 64};
+        for (int x : b)
+            if (nev <= x) return x;
+        return 64;
     }
 
-    // One restart cycle of every active problem with a device operator.
+    // Device part of one cycle: apply pending restarts, extend, (restart), gather.
+    void enqueue_cycle(int steps, int basis_nev) {
+        const int na = (int)active.size();
+        if (!device_restart) launch_scatter(P_d, na, off_d, flag_d, mbox_d, stream);
+        if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), stream);
+        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, s, fp32_any, false, stream);
+        if (device_restart) launch_restart(P_d, na, max_ncv, stream);
+        launch_gather(P_d, na, off_d, mbox_d, stream);
+    }
+
+    int push_mailbox() {
+        const int na = (int)active.size();
+        CK(cudaMemcpyAsync(flag_d, flag_h, sizeof(int) * na, cudaMemcpyHostToDevice, stream));
+        bool any = false;
+        for (int a = 0; a < na; ++a) any = any || flag_h[a];
+        if (any) CK(cudaMemcpyAsync(mbox_d, mbox_h, sizeof(double) * mbox_used, cudaMemcpyHostToDevice, stream));
+        return HLANC_OK;
+    }
+
+    int pull_mailbox() {
+        CK(cudaMemcpyAsync(mbox_h, mbox_d, sizeof(double) * mbox_used, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        CK(cudaGetLastError());
+        for (size_t a = 0; a < active.size(); ++a) {
+            ProbRes &p = probs[active[a]];
+            const double *slot = mbox_h + off_h[a];
+            memcpy(&p.hs, slot, sizeof(State));
+            if (!device_restart) memcpy(p.h.data(), slot + MBOX_STATE, sizeof(double) * 2 * p.ncv);
+        }
+        return HLANC_OK;
+    }
+
+    // One restart cycle of every active device-operator problem.
     int run_cycle(int steps, int basis_nev) {
-        if (!use_graphs) {
+        int rc = push_mailbox();
+        if (rc) return rc;
+        const bool graphs_now = use_graphs && !g_prof;
+        if (!graphs_now) {
             enqueue_cycle(steps, basis_nev);
             CK(cudaGetLastError());
-            return HLANC_OK;
+        } else {
+            const long long key = (long long)steps * 1024 + basis_bucket(basis_nev);
+            auto it = graphs.find(key);
+            if (it == graphs.end()) {
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                enqueue_cycle(steps, basis_nev);
+                CK(cudaStreamEndCapture(stream, &g));
+                cudaGraphExec_t ge;
+                cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+                cudaGraphDestroy(g);
+                CK(e);
+                it = graphs.emplace(key, ge).first;
+            }
+            CK(cudaGraphLaunch(it->second, stream));
         }
-        const long long key = (long long)steps * 1024 + basis_nev;
-        auto it = graphs.find(key);
-        if (it == graphs.end()) {
-            cudaGraph_t g;
-            CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-            enqueue_cycle(steps, basis_nev);
-            CK(cudaStreamEndCapture(stream, &g));
-            cudaGraphExec_t ge;
-            cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
-            cudaGraphDestroy(g);
-            CK(e);
-            it = graphs.emplace(key, ge).first;
-        }
-        CK(cudaGraphLaunch(it->second, stream));
-        return HLANC_OK;
+        for (size_t a = 0; a < active.size(); ++a) probs[active[a]].cycles += 1;
+        return pull_mailbox();
     }
 
     // One restart cycle of a single host-operator problem (synchronous steps).
@@ -353,11 +488,12 @@ public:
             CK(cudaMalloc(&xs_d, sizeof(double) * p.n));
             xs_cap = p.n;
         }
-        if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_nev, stream);
-        int rc = readback();
+        int rc = push_mailbox();
         if (rc) return rc;
-        const int a = slot_of(prob);
-        const int k = st_h[a].k;
+        const int na = (int)active.size();
+        if (!device_restart) launch_scatter(P_d, na, off_d, flag_d, mbox_d, stream);
+        if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), stream);
+        const int k = p.hs.k;
         for (int s = 0; s < steps; ++s) {
             const int j = k + s;
             launch_prep_ext(P_d, T_d, ntiles, s, xs_d, stream);
@@ -368,57 +504,148 @@ public:
             CK(cudaMemcpyAsync(w, ys_h, sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
             launch_step(P_d, T_d, ntiles, s, false, true, stream);
         }
-        launch_restart(P_d, (int)active.size(), max_ncv, stream);
+        if (device_restart) launch_restart(P_d, na, max_ncv, stream);
+        launch_gather(P_d, na, off_d, mbox_d, stream);
         CK(cudaGetLastError());
-        return HLANC_OK;
+        p.cycles += 1;
+        return pull_mailbox();
     }
 
-    // Converged problem -> explicit Q factor and Ritz vectors into p.vout.
-    int finalize(int prob) {
-        ProbRes &p = probs[prob];
-        if (!p.vout) {
-            CK(cudaMalloc(&p.vout, sizeof(double) * (size_t)p.ld * p.ncv));
-            p.own_vout = true;
-            p.ldo = p.ld;
+    // Host restart of every problem whose extension just finished.  Fills the
+    // mailbox for the next cycle; returns the number still running, the
+    // largest nev to apply and the largest np.
+    void host_restarts(int *running, int *nev_max, int *np_max) {
+        *running = 0; *nev_max = 0; *np_max = 0;
+        const double t0 = now_s();
+        for (size_t a = 0; a < active.size(); ++a) {
+            ProbRes &p = probs[active[a]];
+            flag_h[a] = 0;
+            State &S = p.hs;
+            if (device_restart) {
+                if (S.status == ST_RUNNING && S.phase == PH_APPLY) {
+                    ++*running;
+                    *nev_max = std::max(*nev_max, S.nev);
+                    *np_max = std::max(*np_max, S.np);
+                }
+                continue;
+            }
+            if (S.status != ST_RUNNING || S.phase != PH_EXTEND || S.iter < 0) continue;
+            host::RestartIO io;
+            io.ncv = p.ncv; io.nev0 = S.nev0; io.np0 = S.np0; io.max_iter = S.max_iter;
+            io.tol = S.tol; io.eps23 = S.eps23; io.rnorm = S.rnorm; io.iter = S.iter;
+            io.h = p.h.data(); io.ritz_s = p.ritz_s.data(); io.bnds_s = p.bnds_s.data(); io.Q = p.Q.data();
+            const int rs = host::restart(io);
+            S.iter = io.iter;
+            S.nconv = io.nconv;
+            double *slot = mbox_h + off_h[a];
+            if (rs == host::RS_APPLY) {
+                S.nev = io.nev; S.np = io.np; S.k = io.nev; S.phase = PH_APPLY;
+                memcpy(slot + MBOX_STATE, p.h.data(), sizeof(double) * 2 * p.ncv);
+                memcpy(slot + MBOX_STATE + 2 * p.ncv, p.Q.data(), sizeof(double) * p.ncv * p.ncv);
+                flag_h[a] = 1;
+                ++*running;
+                *nev_max = std::max(*nev_max, S.nev);
+                *np_max = std::max(*np_max, S.np);
+            } else {
+                S.status = rs == host::RS_CONVERGED ? ST_CONVERGED
+                         : rs == host::RS_FAILED ? ST_FAILED : ST_NOT_CONVERGED;
+                S.phase = PH_DONE;
+                flag_h[a] = 2;
+            }
+            memcpy(slot, &S, sizeof(State));
         }
-        int rc = upload();
+        if (g_prof) {
+            g_prof->host_ms += (now_s() - t0) * 1e3;
+            g_prof->host_n += 1;
+        }
+    }
+
+    // Converged problems -> values and Ritz vectors (into each p.vout, ldo).
+    int finalize_many(const std::vector<int> &which) {
+        for (int prob : which) {
+            ProbRes &p = probs[prob];
+            if (!p.vout) {
+                CK(cudaMalloc(&p.vout, sizeof(double) * (size_t)p.ld * p.ncv));
+                p.own_vout = true;
+                p.ldo = p.ld;
+            }
+        }
+        int rc = upload();     // descriptors carry vout/ldo
         if (rc) return rc;
-        launch_finalize(P_d, (int)active.size(), max_ncv, stream);
+        if (device_restart) {
+            launch_finalize(P_d, (int)active.size(), max_ncv, stream);
+        } else {
+            for (size_t q = 0; q < active.size(); ++q) flag_h[q] = 0;
+            for (int prob : which) {
+                ProbRes &p = probs[prob];
+                const int a = slot_of(prob);
+                State &S = p.hs;
+                if (S.status != ST_CONVERGED) continue;
+                host::FinalizeIO io;
+                io.ncv = p.ncv; io.nev0 = S.nev0; io.np0 = S.np0; io.nconv = S.nconv;
+                io.tol = S.tol; io.eps23 = S.eps23;
+                io.h = p.h.data(); io.ritz_s = p.ritz_s.data(); io.bnds_s = p.bnds_s.data();
+                io.values = p.values.data();
+                double *slot = mbox_h + off_h[a];
+                io.Q2 = slot + MBOX_STATE + 2 * p.ncv;
+                if (host::finalize(io)) {
+                    S.status = ST_FAILED;
+                    S.fin = 2;
+                    flag_h[a] = 2;
+                } else {
+                    memcpy(slot + MBOX_STATE + 2 * p.ncv + (size_t)p.ncv * p.ncv, p.values.data(),
+                           sizeof(double) * p.ncv);
+                    S.fin = 1;
+                    flag_h[a] = 3;
+                }
+                memcpy(slot, &S, sizeof(State));
+            }
+            if ((rc = push_mailbox())) return rc;
+            launch_scatter(P_d, (int)active.size(), off_d, flag_d, mbox_d, stream);
+        }
         launch_ritz(P_d, T_d, ntiles, max_ncv, stream);
+        launch_gather(P_d, (int)active.size(), off_d, mbox_d, stream);
         CK(cudaGetLastError());
-        return HLANC_OK;
+        for (size_t q = 0; q < active.size(); ++q) flag_h[q] = 0;
+        return pull_mailbox();
+    }
+    int finalize(int prob) { return finalize_many(std::vector<int>{prob}); }
+
+    // Release a finished problem's device memory (serving).
+    void retire(int prob) {
+        probs[prob].release();
+        std::vector<double>().swap(probs[prob].Q);
     }
 };
 
-// Drive one problem (or a whole engine) to completion.  Returns per-problem
-// terminal states in st_h.
-int drive(Engine &E, const std::vector<int> &which) {
-    // first cycle: every problem extends 0..ncv-1
-    int max_steps = 0;
-    for (int p : which) max_steps = std::max(max_steps, E.probs[p].ncv);
+// Run every problem in E.active to a terminal state.
+int drive(Engine &E) {
+    int steps = 0, np0max = 0;
     bool host_path = false;
-    for (int p : which) host_path = host_path || !E.probs[p].csr;
-    int basis_nev = 0;
-    int steps = max_steps;
-    for (;;) {
-        int rc;
-        if (host_path) rc = E.run_cycle_host(which[0], steps, basis_nev);
-        else rc = E.run_cycle(steps, basis_nev);
-        if (rc) return rc;
-        if ((rc = E.readback())) return rc;
-        int running = 0, nmax = 0, stepmax = 0;
-        for (size_t a = 0; a < E.active.size(); ++a) {
-            const State &S = E.st_h[a];
-            if (S.status == ST_RUNNING && S.phase == PH_APPLY) {
-                ++running;
-                nmax = std::max(nmax, S.nev);
-                stepmax = std::max(stepmax, S.np);
-            }
-        }
-        if (!running) break;
-        basis_nev = nmax;
-        steps = stepmax;
+    for (int p : E.active) {
+        steps = std::max(steps, E.probs[p].ncv);
+        np0max = std::max(np0max, E.probs[p].ncv - E.probs[p].nev0);
+        host_path = host_path || !E.probs[p].csr;
     }
+    int basis_nev = 0;
+    for (;;) {
+        int rc = host_path ? E.run_cycle_host(E.active[0], steps, basis_nev) : E.run_cycle(steps, basis_nev);
+        if (rc) return rc;
+        int running, nev_max, np_max;
+        E.host_restarts(&running, &nev_max, &np_max);
+        if (!running) break;
+        basis_nev = nev_max;
+        // later cycles launch the largest possible extension (np0 steps);
+        // steps beyond a problem's current np exit at once on the device, so
+        // one captured graph serves every cycle
+        steps = host_path ? np_max : np0max;
+    }
+    // push terminal states to the device
+    int rc = E.push_mailbox();
+    if (rc) return rc;
+    if (!E.device_restart) launch_scatter(E.P_d, (int)E.active.size(), E.off_d, E.flag_d, E.mbox_d, E.stream);
+    for (size_t a = 0; a < E.active.size(); ++a) E.flag_h[a] = 0;
+    CK(cudaStreamSynchronize(E.stream));
     return HLANC_OK;
 }
 
@@ -442,13 +669,31 @@ void fill_stats(hlanc_stats_t *stats, const State &S, const ProbRes &p, double n
     stats->bytes_restart = (8.0 * n * p.ncv + 16.0 * n) * S.napply + 8.0 * n * (double)S.sumnev;
 }
 
-int map_status(int st) {
-    switch (st) {
-    case ST_CONVERGED: return HLANC_OK;
-    case ST_NOT_CONVERGED: return HLANC_NOT_CONVERGED;
-    case ST_FAILED: return HLANC_NOT_CONVERGED;
-    default: return HLANC_NOT_CONVERGED;
+void fill_profile(const State &S, const ProbRes &p, double nnz, int fp32) {
+    if (!g_prof) return;
+    hlanc_profile_t &P = g_last_prof;
+    memset(&P, 0, sizeof P);
+    cudaDeviceSynchronize();
+    for (auto &r : g_prof->recs) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        P.launches[r.cls] += 1;
+        P.ms[r.cls] += ms;
     }
+    const double n = p.n, m = p.ncv;
+    P.bytes[KC_SPMV] = (fp32 ? (8.0 * nnz + 4.0 * (n + 1) + 24.0 * n) : (12.0 * nnz + 4.0 * (n + 1) + 32.0 * n)) * S.spmv;
+    P.flops[KC_SPMV] = 2.0 * nnz * S.spmv;
+    P.bytes[KC_PROJ] = 8.0 * n * S.sumc + 8.0 * n * S.passes;
+    P.flops[KC_PROJ] = 2.0 * n * S.sumc;
+    P.bytes[KC_APPLY] = 8.0 * n * S.sumc + 16.0 * n * S.passes;
+    P.flops[KC_APPLY] = 2.0 * n * S.sumc + 2.0 * n * S.passes;
+    P.bytes[KC_BASIS] = (8.0 * n * m + 16.0 * n) * S.napply + 8.0 * n * S.sumnev;
+    P.flops[KC_BASIS] = 2.0 * n * m * (S.sumnev + S.napply);
+    P.bytes[KC_RITZ] = 16.0 * n * m;
+    P.flops[KC_RITZ] = 2.0 * n * m * m;
+    P.launches[KC_HOST] = g_prof->host_n;
+    P.ms[KC_HOST] = g_prof->host_ms;
+    g_have_prof = true;
 }
 
 __global__ void k_sum_columns(const double *__restrict__ Y, int ld, int n, int k, double *__restrict__ out) {
@@ -459,45 +704,57 @@ __global__ void k_sum_columns(const double *__restrict__ Y, int ld, int n, int k
     }
 }
 
-// Full solve of one problem on an engine.  values_out/vectors_out are host
-// (device_out = false) or device pointers.
+int map_status(int st) { return st == ST_CONVERGED ? HLANC_OK : HLANC_NOT_CONVERGED; }
+
+// Full solve of one problem.  values/vectors are host (device_out = false)
+// or device pointers.
 int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors, int ldv, bool device_out,
               hlanc_csr_s *csr, hlanc_host_op_fn host_op, void *host_ctx, const hlanc_opts_t &o,
               hlanc_stats_t *stats) {
     const double t0 = now_s();
     DevGuard g(dev);
+    std::unique_ptr<Profiler> prof;
+    if (o.profile) {
+        prof.reset(new Profiler());
+        g_prof = prof.get();
+    }
+    struct ProfReset { ~ProfReset() { g_prof = nullptr; } } prof_reset;
     Engine E;
-    int rc = E.init(dev, o.stream, o.use_graphs != 0);
+    int rc = E.init(dev, o.stream, o.use_graphs != 0, o.restart_on_device != 0);
     if (rc) return rc;
     const bool fp32 = csr && o.precision == HLANC_PREC_FP32_REFINE && csr->val32_d;
     int idx = 0;
-    // phase 1: FP32 SpMV to a loose tolerance when mixed precision is asked for
     hlanc_opts_t o1 = o;
-    if (fp32) o1.tol = std::max(o.tol > 0 ? o.tol : 0.0, 1e-6);
+    if (fp32) o1.tol = std::max(o.tol > 0 ? o.tol : 0.0, 1e-6);   // FP32 phase: loose tolerance
     rc = E.add(n, nev, ncv, csr, host_op, host_ctx, fp32 ? 1 : 0, o1, &idx);
     if (rc) return rc;
     E.active = {idx};
     if ((rc = E.upload())) return rc;
     if ((rc = E.start_vector(idx, o))) return rc;
-    if ((rc = drive(E, E.active))) return rc;
-    State S1 = E.st_h[0];
+    if ((rc = E.norm_init())) return rc;
+    if ((rc = drive(E))) return rc;
+    ProbRes &p = E.probs[idx];
+    State S1 = p.hs;
     int refine_restarts = 0;
     State S = S1;
     if (fp32) {
-        // phase 2: FP64 restarts warm-started from the sum of the FP32 Ritz vectors
-        ProbRes &p = E.probs[idx];
-        if (S1.status == ST_CONVERGED) {
+        // FP64 phase warm-started from the sum of the FP32 Ritz vectors
+        const bool warm = S1.status == ST_CONVERGED;
+        if (warm) {
             if ((rc = E.finalize(idx))) return rc;
             k_sum_columns<<<304, 256, 0, E.stream>>>(p.vout, p.ldo, p.n, S1.nconv, p.r0);
             launch_counter() += 1;
         }
         State S0 = initial_state(nev, ncv, o);
+        p.hs = S0;
+        p.cycles = 0;
         CK(cudaMemcpyAsync(p.st, &S0, sizeof S0, cudaMemcpyHostToDevice, E.stream));
         p.fp32 = 0;
         if ((rc = E.upload())) return rc;
-        launch_norm_init(E.P_d, E.T_d, E.ntiles, E.stream);
-        if ((rc = drive(E, E.active))) return rc;
-        S = E.st_h[0];
+        if (!warm && (rc = E.start_vector(idx, o))) return rc;
+        if ((rc = E.norm_init())) return rc;
+        if ((rc = drive(E))) return rc;
+        S = p.hs;
         refine_restarts = S.iter;
         S.spmv += S1.spmv;
         S.passes += S1.passes;
@@ -507,7 +764,6 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
     }
     int status = map_status(S.status);
     if (S.status == ST_CONVERGED) {
-        ProbRes &p = E.probs[idx];
         if (device_out) {
             if (p.own_vout && p.vout) cudaFree(p.vout);
             p.vout = vectors;
@@ -515,12 +771,11 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
             p.own_vout = false;
         }
         if ((rc = E.finalize(idx))) return rc;
-        if ((rc = E.readback())) return rc;
-        if (E.st_h[0].status != ST_CONVERGED) {
+        if (p.hs.status != ST_CONVERGED) {
             status = HLANC_NOT_CONVERGED;
         } else {
             const int m = p.ncv;
-            const int nconv = E.st_h[0].nconv;
+            const int nconv = p.hs.nconv;
             if (device_out) {
                 CK(cudaMemcpyAsync(values, p.small + SM_VALS(m), sizeof(double) * nconv, cudaMemcpyDeviceToDevice, E.stream));
             } else {
@@ -532,8 +787,9 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
         }
     }
     const double nnz = csr ? (double)csr->nnz : 0.0;
-    fill_stats(stats, S, E.probs[idx], nnz, fp32 ? 1 : 0, refine_restarts, now_s() - t0, status);
+    fill_stats(stats, S, p, nnz, fp32 ? 1 : 0, refine_restarts, now_s() - t0, status);
     if (stats && S.status == ST_CONVERGED) stats->bytes_restart += 16.0 * n * ncv;
+    fill_profile(S, p, nnz, fp32 ? 1 : 0);
     return status;
 }
 
@@ -583,6 +839,14 @@ void hlanc_opts_default(hlanc_opts_t *o) {
     o->start = nullptr;
     o->stream = nullptr;
     o->use_graphs = 1;
+    o->restart_on_device = 0;
+    o->profile = 0;
+}
+
+int hlanc_last_profile(hlanc_profile_t *out) {
+    if (!out || !g_have_prof) return HLANC_ERR_INVALID;
+    *out = g_last_prof;
+    return HLANC_OK;
 }
 
 // ---- host matrices -------------------------------------------------------------
@@ -836,6 +1100,381 @@ int hlanc_residuals_device(hlanc_csr_t csr, int k, const double *values_d, const
         if (resid_h) resid_h[i] = sqrt(h[4 * i]);
         const double mx = std::max(h[4 * i + 2], h[4 * i + 3]);
         if (rdiff_h) rdiff_h[i] = mx > 0 ? h[4 * i + 1] / mx : h[4 * i + 1];
+    }
+    return HLANC_OK;
+}
+
+
+// ---- batched solves ------------------------------------------------------------------
+}  // extern "C"
+
+struct hlanc_batch_s {
+    Engine E;
+    std::vector<int> idx;
+    std::vector<hlanc_csr_s *> ops;
+    std::vector<int> nev, ncv;
+    hlanc_opts_t o;
+    int dev = 0;
+};
+
+namespace {
+
+// Drive a set of problems; with FP32 operators, a second FP64 phase starts
+// each from the sum of its FP32 Ritz vectors (or a fresh start vector).
+int run_problems(Engine &E, const std::vector<int> &idx, const std::vector<int> &nev, const std::vector<int> &ncv,
+                 const hlanc_opts_t &o, bool fp32, std::vector<State> &first_phase) {
+    int rc;
+    E.active = idx;
+    if ((rc = E.upload())) return rc;
+    for (int p : idx)
+        if ((rc = E.start_vector(p, o))) return rc;
+    if ((rc = E.norm_init())) return rc;
+    if ((rc = drive(E))) return rc;
+    first_phase.clear();
+    for (int p : idx) first_phase.push_back(E.probs[p].hs);
+    if (!fp32) return HLANC_OK;
+    std::vector<int> conv;
+    for (int p : idx)
+        if (E.probs[p].hs.status == ST_CONVERGED) conv.push_back(p);
+    if (!conv.empty() && (rc = E.finalize_many(conv))) return rc;
+    for (size_t q = 0; q < idx.size(); ++q) {
+        ProbRes &p = E.probs[idx[q]];
+        if (p.hs.status == ST_CONVERGED) {
+            k_sum_columns<<<304, 256, 0, E.stream>>>(p.vout, p.ldo, p.n, p.hs.nconv, p.r0);
+            launch_counter() += 1;
+        }
+        const bool warm = p.hs.status == ST_CONVERGED;
+        State S0 = initial_state(nev[q], ncv[q], o);
+        p.hs = S0;
+        p.cycles = 0;
+        p.fp32 = 0;
+        CK(cudaMemcpyAsync(p.st, &S0, sizeof S0, cudaMemcpyHostToDevice, E.stream));
+        if (!warm) p.cycles = -1;   // marks "needs a fresh start vector"
+    }
+    if ((rc = E.upload())) return rc;
+    for (int p : idx)
+        if (E.probs[p].cycles == -1) {
+            E.probs[p].cycles = 0;
+            if ((rc = E.start_vector(p, o))) return rc;
+        }
+    if ((rc = E.norm_init())) return rc;
+    return drive(E);
+}
+
+}  // namespace
+
+extern "C" {
+
+int hlanc_batch_create(int dev, int nprob, const hlanc_csr_t *ops, const int *nev, const int *ncv,
+                       const hlanc_opts_t *opts, hlanc_batch_t *out) {
+    if (nprob <= 0 || !ops || !nev || !ncv || !out) return HLANC_ERR_INVALID;
+    std::unique_ptr<hlanc_batch_s> b(new hlanc_batch_s());
+    if (opts) b->o = *opts;
+    else hlanc_opts_default(&b->o);
+    b->dev = dev;
+    DevGuard g(dev);
+    int rc = b->E.init(dev, b->o.stream, b->o.use_graphs != 0, b->o.restart_on_device != 0);
+    if (rc) return rc;
+    const bool fp32 = b->o.precision == HLANC_PREC_FP32_REFINE;
+    hlanc_opts_t o1 = b->o;
+    if (fp32) o1.tol = std::max(b->o.tol > 0 ? b->o.tol : 0.0, 1e-6);
+    for (int i = 0; i < nprob; ++i) {
+        hlanc_csr_s *c = ops[i];
+        if (!c || c->dev != dev) return HLANC_ERR_INVALID;
+        if ((rc = validate(c->nrows, nev[i], ncv[i], c->nrows))) return rc;
+        if (c->ncols > c->nrows) return HLANC_ERR_INVALID;
+        if (fp32 && !c->val32_d) return HLANC_ERR_INVALID;
+        int idx = 0;
+        if ((rc = b->E.add(c->nrows, nev[i], ncv[i], c, nullptr, nullptr, fp32 ? 1 : 0, o1, &idx))) return rc;
+        b->idx.push_back(idx);
+        b->ops.push_back(c);
+        b->nev.push_back(nev[i]);
+        b->ncv.push_back(ncv[i]);
+    }
+    *out = b.release();
+    return HLANC_OK;
+}
+
+int hlanc_batch_run(hlanc_batch_t b, double **values_d, double **vectors_d, int *status, hlanc_stats_t *stats) {
+    if (!b || !values_d || !vectors_d) return HLANC_ERR_INVALID;
+    const double t0 = now_s();
+    DevGuard g(b->dev);
+    std::unique_ptr<Profiler> prof;
+    if (b->o.profile) {
+        prof.reset(new Profiler());
+        g_prof = prof.get();
+    }
+    struct ProfReset { ~ProfReset() { g_prof = nullptr; } } prof_reset;
+    Engine &E = b->E;
+    const bool fp32 = b->o.precision == HLANC_PREC_FP32_REFINE;
+    std::vector<State> first;
+    int rc = run_problems(E, b->idx, b->nev, b->ncv, b->o, fp32, first);
+    if (rc) return rc;
+    std::vector<int> conv;
+    for (size_t q = 0; q < b->idx.size(); ++q) {
+        ProbRes &p = E.probs[b->idx[q]];
+        if (p.own_vout && p.vout) cudaFree(p.vout);
+        p.vout = vectors_d[q];
+        p.ldo = p.n;
+        p.own_vout = false;
+        if (p.hs.status == ST_CONVERGED) conv.push_back(b->idx[q]);
+    }
+    if (!conv.empty() && (rc = E.finalize_many(conv))) return rc;
+    long long spmv = 0, passes = 0;
+    int ok = 0, restarts = 0;
+    double by_spmv = 0, by_cgs = 0, by_rs = 0;
+    for (size_t q = 0; q < b->idx.size(); ++q) {
+        ProbRes &p = E.probs[b->idx[q]];
+        State S = p.hs;
+        if (fp32) {
+            S.spmv += first[q].spmv; S.passes += first[q].passes; S.sumc += first[q].sumc;
+            S.sumnev += first[q].sumnev; S.napply += first[q].napply;
+        }
+        const int st = map_status(S.status);
+        if (status) status[q] = st;
+        if (S.status == ST_CONVERGED) {
+            ++ok;
+            CK(cudaMemcpyAsync(values_d[q], p.small + SM_VALS(p.ncv), sizeof(double) * S.nconv,
+                               cudaMemcpyDeviceToDevice, E.stream));
+        }
+        hlanc_stats_t one;
+        fill_stats(&one, S, p, (double)b->ops[q]->nnz, fp32 ? 1 : 0, 0, 0.0, st);
+        spmv += one.spmv_calls; passes += one.cgs_passes; restarts = std::max(restarts, one.restarts);
+        by_spmv += one.bytes_spmv; by_cgs += one.bytes_cgs; by_rs += one.bytes_restart;
+    }
+    CK(cudaStreamSynchronize(E.stream));
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->spmv_calls = spmv; stats->cgs_passes = passes; stats->restarts = restarts;
+        stats->nconv = ok; stats->status = ok == (int)b->idx.size() ? HLANC_OK : HLANC_NOT_CONVERGED;
+        stats->seconds = now_s() - t0;
+        stats->bytes_spmv = by_spmv; stats->bytes_cgs = by_cgs; stats->bytes_restart = by_rs;
+    }
+    return ok == (int)b->idx.size() ? HLANC_OK : HLANC_NOT_CONVERGED;
+}
+
+int hlanc_batch_destroy(hlanc_batch_t b) {
+    if (!b) return HLANC_OK;
+    int dev = b->dev;
+    {
+        DevGuard g(dev);
+        delete b;
+    }
+    return HLANC_OK;
+}
+
+}  // extern "C"
+
+// ---- serving: continuous batching --------------------------------------------------
+struct hlanc_server_s {
+    struct Request {
+        long long id = 0;
+        hlanc_csr_s *csr = nullptr;
+        int nev = 0, ncv = 0;
+        hlanc_opts_t o;
+        int state = 0;           // 0 pending, 1 active, 2 done
+        int status = HLANC_OK;
+        int prob = -1;
+        size_t bytes = 0;
+        bool cancel = false;
+        std::vector<double> values, vectors;
+        hlanc_stats_t stats;
+        double t_submit = 0, t_admit = 0, t_done = 0;
+        std::vector<double> start;
+    };
+    hlanc_server_opts_t opts;
+    Engine E;
+    std::map<long long, Request> reqs;
+    std::deque<long long> pending;
+    std::vector<long long> active;   // request ids, engine problems in E.active
+    size_t used = 0;
+    long long next_id = 1;
+    std::mutex mu;
+};
+
+extern "C" {
+
+int hlanc_server_create(const hlanc_server_opts_t *opts, hlanc_server_t *out) {
+    if (!opts || !out || opts->max_slots <= 0) return HLANC_ERR_INVALID;
+    std::unique_ptr<hlanc_server_s> s(new hlanc_server_s());
+    s->opts = *opts;
+    DevGuard g(opts->dev);
+    int rc = s->E.init(opts->dev, nullptr, false, false);   // eager launches: the active set changes every tick
+    if (rc) return rc;
+    *out = s.release();
+    return HLANC_OK;
+}
+
+int hlanc_server_submit(hlanc_server_t s, hlanc_csr_t csr, int nev, int ncv, const hlanc_opts_t *opts,
+                        long long *request_id) {
+    if (!s || !csr || !request_id) return HLANC_ERR_INVALID;
+    int rc = validate(csr->nrows, nev, ncv, csr->nrows);
+    if (rc) return rc;
+    if (csr->dev != s->opts.dev || csr->ncols > csr->nrows) return HLANC_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    hlanc_server_s::Request r;
+    r.id = s->next_id++;
+    r.csr = csr;
+    r.nev = nev;
+    r.ncv = ncv;
+    if (opts) r.o = *opts;
+    else hlanc_opts_default(&r.o);
+    if (r.o.start) r.start.assign(r.o.start, r.o.start + csr->nrows);
+    r.o.start = nullptr;
+    r.o.precision = HLANC_PREC_FP64;
+    r.bytes = ProbRes::estimate(csr->nrows, ncv, 0);
+    if (r.bytes > s->opts.mem_budget_bytes) return HLANC_ERR_ALLOC;
+    r.t_submit = now_s();
+    memset(&r.stats, 0, sizeof r.stats);
+    *request_id = r.id;
+    s->pending.push_back(r.id);
+    s->reqs.emplace(r.id, std::move(r));
+    return HLANC_OK;
+}
+
+// One scheduler tick: admit what fits, run one restart cycle of every
+// resident solve (their launches share one sequence), retire finished ones.
+int hlanc_server_step(hlanc_server_t s, int *n_active, int *n_pending) {
+    if (!s) return HLANC_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    DevGuard g(s->opts.dev);
+    Engine &E = s->E;
+    int rc;
+    // cancellations
+    for (auto it = s->active.begin(); it != s->active.end();) {
+        auto &r = s->reqs[*it];
+        if (r.cancel) {
+            E.retire(r.prob);
+            s->used -= r.bytes;
+            r.state = 2; r.status = HLANC_ERR_CANCELLED; r.t_done = now_s();
+            it = s->active.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    // admission by slots and memory budget (CSR resident already; basis + workspace)
+    std::vector<long long> admitted;
+    while (!s->pending.empty() && (int)s->active.size() < s->opts.max_slots) {
+        auto &r = s->reqs[s->pending.front()];
+        if (r.cancel) {
+            r.state = 2; r.status = HLANC_ERR_CANCELLED; r.t_done = now_s();
+            s->pending.pop_front();
+            continue;
+        }
+        if (s->used + r.bytes > s->opts.mem_budget_bytes) break;
+        int idx = 0;
+        if ((rc = E.add(r.csr->nrows, r.nev, r.ncv, r.csr, nullptr, nullptr, 0, r.o, &idx))) return rc;
+        r.prob = idx;
+        r.state = 1;
+        r.t_admit = now_s();
+        s->used += r.bytes;
+        s->active.push_back(r.id);
+        admitted.push_back(r.id);
+        s->pending.pop_front();
+    }
+    if (s->active.empty()) {
+        if (n_active) *n_active = 0;
+        if (n_pending) *n_pending = (int)s->pending.size();
+        return HLANC_OK;
+    }
+    // launch tables: active problems in request order; keep mailbox state
+    std::vector<State> keep;
+    E.active.clear();
+    for (long long id : s->active) E.active.push_back(s->reqs[id].prob);
+    if ((rc = E.upload())) return rc;
+    // restarts decided at the previous tick are re-armed in the mailbox
+    for (size_t a = 0; a < E.active.size(); ++a) {
+        ProbRes &p = E.probs[E.active[a]];
+        E.flag_h[a] = 0;
+        if (p.cycles > 0 && p.hs.status == ST_RUNNING && p.hs.phase == PH_APPLY) {
+            double *slot = E.mbox_h + E.off_h[a];
+            memcpy(slot, &p.hs, sizeof(State));
+            memcpy(slot + MBOX_STATE, p.h.data(), sizeof(double) * 2 * p.ncv);
+            memcpy(slot + MBOX_STATE + 2 * p.ncv, p.Q.data(), sizeof(double) * p.ncv * p.ncv);
+            E.flag_h[a] = 1;
+        }
+    }
+    for (long long id : admitted) {
+        auto &r = s->reqs[id];
+        hlanc_opts_t o = r.o;
+        if (!r.start.empty()) o.start = r.start.data();
+        if ((rc = E.start_vector(r.prob, o))) return rc;
+    }
+    if (!admitted.empty() && (rc = E.norm_init())) return rc;
+    int steps = 0, basis_nev = 0;
+    for (int pi : E.active) {
+        ProbRes &p = E.probs[pi];
+        steps = std::max(steps, p.cycles == 0 ? p.ncv : p.ncv - p.nev0);
+        if (p.cycles > 0 && p.hs.phase == PH_APPLY) basis_nev = std::max(basis_nev, p.hs.nev);
+    }
+    if ((rc = E.run_cycle(steps, basis_nev))) return rc;
+    int running, nev_max, np_max;
+    E.host_restarts(&running, &nev_max, &np_max);
+    // retire finished solves
+    std::vector<int> conv;
+    for (long long id : s->active) {
+        auto &r = s->reqs[id];
+        ProbRes &p = E.probs[r.prob];
+        if (p.hs.status != ST_RUNNING && p.hs.status == ST_CONVERGED) conv.push_back(r.prob);
+    }
+    if (!conv.empty() && (rc = E.finalize_many(conv))) return rc;
+    for (auto it = s->active.begin(); it != s->active.end();) {
+        auto &r = s->reqs[*it];
+        ProbRes &p = E.probs[r.prob];
+        if (p.hs.status == ST_RUNNING) { ++it; continue; }
+        r.status = map_status(p.hs.status);
+        if (p.hs.status == ST_CONVERGED) {
+            const int n = p.n, m = p.ncv;
+            r.values.assign(p.values.begin(), p.values.begin() + p.hs.nconv);
+            r.vectors.resize((size_t)n * m);
+            CK(cudaMemcpy2DAsync(r.vectors.data(), sizeof(double) * n, p.vout, sizeof(double) * p.ldo,
+                                 sizeof(double) * n, m, cudaMemcpyDeviceToHost, E.stream));
+            CK(cudaStreamSynchronize(E.stream));
+        }
+        fill_stats(&r.stats, p.hs, p, (double)r.csr->nnz, 0, 0, 0.0, r.status);
+        r.t_done = now_s();
+        r.stats.seconds = r.t_done - r.t_submit;
+        r.state = 2;
+        E.retire(r.prob);
+        s->used -= r.bytes;
+        it = s->active.erase(it);
+    }
+    if (n_active) *n_active = (int)s->active.size();
+    if (n_pending) *n_pending = (int)s->pending.size();
+    return HLANC_OK;
+}
+
+int hlanc_server_poll(hlanc_server_t s, long long request_id, int *done, int *status, double *values,
+                      double *vectors, hlanc_stats_t *stats) {
+    if (!s || !done) return HLANC_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(request_id);
+    if (it == s->reqs.end()) return HLANC_ERR_INVALID;
+    auto &r = it->second;
+    *done = r.state == 2;
+    if (!*done) return HLANC_OK;
+    if (status) *status = r.status;
+    if (values && !r.values.empty()) memcpy(values, r.values.data(), sizeof(double) * r.values.size());
+    if (vectors && !r.vectors.empty()) memcpy(vectors, r.vectors.data(), sizeof(double) * r.vectors.size());
+    if (stats) *stats = r.stats;
+    return HLANC_OK;
+}
+
+int hlanc_server_cancel(hlanc_server_t s, long long request_id) {
+    if (!s) return HLANC_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(request_id);
+    if (it == s->reqs.end()) return HLANC_ERR_INVALID;
+    if (it->second.state != 2) it->second.cancel = true;
+    return HLANC_OK;
+}
+
+int hlanc_server_destroy(hlanc_server_t s) {
+    if (!s) return HLANC_OK;
+    const int dev = s->opts.dev;
+    {
+        DevGuard g(dev);
+        delete s;
     }
     return HLANC_OK;
 }

@@ -72,11 +72,12 @@ struct Problem {
     int n, ld, ncv, nev0;
     int tile0, ntiles;
     int fp32;              // SpMV on FP32 values/vectors
-    int pstride;           // doubles per tile partial slot
+    int pstride;           // values per tile partial slot (part is pstride x ntiles, value-major)
     double *V;
     double *r0, *r1;
-    double *part;
-    unsigned *counter;
+    double *part;          // tile partial sums, value-major (pstride x ntiles)
+    double *gpart;         // group partial sums, value-major (pstride x ngroups)
+    unsigned *counter;     // [0] problem counter, [1 + g] group counters
     State *st;
     double *small;
     const double *wext;    // non-null: operator output is supplied by the host callback path
@@ -98,46 +99,114 @@ __device__ __forceinline__ float warp_sum_f(float v) {
     return v;
 }
 
-// Write this tile's nv partial sums (smem `mine`) to its slot, then let the
-// last CTA of the problem sum all slots in tile order into smem `total`.
-// Returns true (in every thread of that CTA) for the last CTA only.
+// Reduce 8 values per lane across the warp ("transposed" butterfly): 9
+// FP64 adds per lane instead of 8 x 5.  On return lane l holds the warp sum
+// of value q = l >> 2 (lanes 4q..4q+3 hold the same value).  Fixed order,
+// so results are deterministic.
+__device__ __forceinline__ double warp_reduce8(double a[8]) {
+    const int lane = threadIdx.x & 31;
+    const bool b4 = lane & 16;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const double keep = b4 ? a[q + 4] : a[q];
+        const double send = b4 ? a[q] : a[q + 4];
+        a[q] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+    const bool b3 = lane & 8;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const double keep = b3 ? a[q + 2] : a[q];
+        const double send = b3 ? a[q] : a[q + 2];
+        a[q] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    const bool b2 = lane & 4;
+    {
+        const double keep = b2 ? a[1] : a[0];
+        const double send = b2 ? a[0] : a[1];
+        a[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    double v = a[0];
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    // lane l now holds value index b4*4 + b3*2 + b2 = l >> 2
+    return v;
+}
+
+// Sum `cnt` slots src[i * stride + t], t < cnt, for i < nv into dst[i]
+// (smem), in a fixed order; the whole CTA cooperates, 8 values per warp.
+__device__ __forceinline__ void reduce_slots(const double *src, int stride, int cnt, int nv,
+                                             double *dst) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i0 = warp * 8; i0 < nv; i0 += nw * 8) {
+        double a[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[q] = 0.0;
+        for (int t = lane; t < cnt; t += 32) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (i0 + q < nv) a[q] += __ldcg(src + (size_t)(i0 + q) * stride + t);
+        }
+        const double v = warp_reduce8(a);
+        const int q = lane >> 2;
+        if ((lane & 3) == 0 && i0 + q < nv) dst[i0 + q] = v;
+    }
+}
+
+// Write this tile's nv partial sums (smem `mine`), then reduce in two
+// levels: the last tile CTA of each group of 32 tiles sums its group, the
+// last group sums the group results into smem `total`.  Returns true (in
+// every thread of that CTA) for the CTA holding the final sums.  Slots are
+// value-major (part[i * ntiles + tile]) so the reads are coalesced.
+constexpr int RGROUP = 32;
 __device__ __forceinline__ bool finish_tile(const Problem &P, int tl, int nv, const double *mine,
                                             double *total) {
     __shared__ unsigned s_ticket;
-    double *slot = P.part + (size_t)tl * P.pstride;
-    for (int i = threadIdx.x; i < nv; i += blockDim.x) slot[i] = mine[i];
+    const int nt = P.ntiles;
+    const int ng = (nt + RGROUP - 1) / RGROUP;
+    const int g = tl / RGROUP;
+    const int gcnt = min(RGROUP, nt - g * RGROUP);
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) P.part[(size_t)i * nt + tl] = mine[i];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_ticket = atomicAdd(P.counter + 1 + g, 1u);
+    __syncthreads();
+    if (s_ticket != (unsigned)(gcnt - 1)) return false;
+    __threadfence();
+    reduce_slots(P.part + (size_t)g * RGROUP, nt, gcnt, nv, total);
+    __syncthreads();
+    if (threadIdx.x == 0) P.counter[1 + g] = 0u;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) P.gpart[(size_t)i * ng + g] = total[i];
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) s_ticket = atomicAdd(P.counter, 1u);
     __syncthreads();
-    if (s_ticket != (unsigned)(P.ntiles - 1)) return false;
+    if (s_ticket != (unsigned)(ng - 1)) return false;
     __threadfence();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int i = warp; i < nv; i += nw) {
-        double s = 0.0;
-        for (int t = lane; t < P.ntiles; t += 32) s += __ldcg(P.part + (size_t)t * P.pstride + i);
-        s = warp_sum(s);
-        if (lane == 0) total[i] = s;
-    }
+    reduce_slots(P.gpart, ng, ng, nv, total);
     __syncthreads();
     if (threadIdx.x == 0) *P.counter = 0u;
     return true;
 }
 
-// CTA-wide sum of one value per thread (deterministic), result in every thread.
-__device__ __forceinline__ double block_sum(double v, double *scratch /* >= 32 */) {
+// CTA-wide sum of one value per thread (deterministic); valid in thread 0.
+__device__ __forceinline__ double block_sum0(double v, double *scratch /* >= 32 */) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     v = warp_sum(v);
-    __syncthreads();
     if (lane == 0) scratch[warp] = v;
     __syncthreads();
     double s = 0.0;
-    for (int w = 0; w < nw; ++w) s += scratch[w];
+    if (threadIdx.x == 0)
+        for (int w = 0; w < nw; ++w) s += scratch[w];
     return s;
 }
 
 __device__ __forceinline__ const double *step_in(const Problem &P, int j) { return (j & 1) ? P.r1 : P.r0; }
 __device__ __forceinline__ double *step_out(const Problem &P, int j) { return (j & 1) ? P.r0 : P.r1; }
+
+// ---- launch profiling (engine.cu): CUDA events around each launch ---------
+enum : int { KC_SPMV = 0, KC_PROJ = 1, KC_APPLY = 2, KC_BASIS = 3, KC_RITZ = 4, KC_AUX = 5, KC_HOST = 6 };
+void prof_begin(cudaStream_t s);
+void prof_end(int cls, cudaStream_t s);
 
 // ---- kernel entry points (kernels_step.cu / kernels_restart.cu) -----------
 void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, int prob,
@@ -157,6 +226,9 @@ void launch_spmv(const int *row_ptr, const int *col, const double *val, int nrow
                  double *y, cudaStream_t s);
 void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, int nrows,
                      const float *x, float *y, cudaStream_t s);
+void launch_gather(const Problem *P_d, int nprob, const long long *off_d, double *buf_d, cudaStream_t s);
+void launch_scatter(const Problem *P_d, int nprob, const long long *off_d, const int *flag_d,
+                    const double *buf_d, cudaStream_t s);
 void launch_residuals(const int *row_ptr, const int *col, const double *val, int n, int k,
                       const double *values_d, const double *vectors_d, int ldv, double *out4k,
                       cudaStream_t s);

@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(TPB) k_basis(const Problem *__restrict__ probs
         rout[r] = res;
         nrm = fma(res, res, nrm);
     }
-    nrm = block_sum(nrm, scratch);
+    nrm = block_sum0(nrm, scratch);
     if (threadIdx.x == 0) mine[0] = nrm;
     __syncthreads();
     if (!finish_tile(P, blockIdx.x - P.tile0, 1, mine, tot)) return;
@@ -591,9 +591,61 @@ __global__ void __launch_bounds__(TPB) k_ritz(const Problem *__restrict__ probs,
     if (threadIdx.x == 0) S->fin = 2;
 }
 
+// ---- host-restart mailbox: one gather / one scatter per cycle -----------------
+// Per problem a, at off[a] (doubles): [State (32 doubles) | h (2m) | Q (m*m) | values (m)].
+static_assert(sizeof(State) <= 32 * sizeof(double), "State must fit its mailbox slot");
+
+__global__ void k_gather(const Problem *__restrict__ probs, const long long *__restrict__ off,
+                         double *__restrict__ buf) {
+    const Problem &P = probs[blockIdx.x];
+    double *o = buf + off[blockIdx.x];
+    const double *st = reinterpret_cast<const double *>(P.st);
+    const int ns = (int)(sizeof(State) / sizeof(double));
+    for (int i = threadIdx.x; i < ns; i += blockDim.x) o[i] = st[i];
+    for (int i = threadIdx.x; i < 2 * P.ncv; i += blockDim.x) o[32 + i] = P.small[SM_H(P.ncv) + i];
+}
+
+// flag 1: State + h + Q (a restart to apply); 2: State only; 3: State + Q2 +
+// values (finalised pair set); 0: nothing.
+__global__ void k_scatter(const Problem *__restrict__ probs, const long long *__restrict__ off,
+                          const int *__restrict__ flag, const double *__restrict__ buf) {
+    const int f = flag[blockIdx.x];
+    if (!f) return;
+    const Problem &P = probs[blockIdx.x];
+    const int m = P.ncv;
+    const double *in = buf + off[blockIdx.x];
+    double *st = reinterpret_cast<double *>(P.st);
+    const int ns = (int)(sizeof(State) / sizeof(double));
+    for (int i = threadIdx.x; i < ns; i += blockDim.x) st[i] = in[i];
+    if (f == 1) {
+        for (int i = threadIdx.x; i < 2 * m; i += blockDim.x) P.small[SM_H(m) + i] = in[32 + i];
+        for (int i = threadIdx.x; i < m * m; i += blockDim.x) P.small[SM_Q(m) + i] = in[32 + 2 * m + i];
+    } else if (f == 3) {
+        for (int i = threadIdx.x; i < m * m; i += blockDim.x) P.small[SM_Q2(m) + i] = in[32 + 2 * m + i];
+        for (int i = threadIdx.x; i < m; i += blockDim.x) P.small[SM_VALS(m) + i] = in[32 + 2 * m + m * m + i];
+    }
+}
+
 // ---- launchers -------------------------------------------------------------------
+void launch_gather(const Problem *P_d, int nprob, const long long *off_d, double *buf_d, cudaStream_t s) {
+    prof_begin(s);
+    k_gather<<<nprob, 128, 0, s>>>(P_d, off_d, buf_d);
+    prof_end(KC_AUX, s);
+    launch_counter() += 1;
+}
+
+void launch_scatter(const Problem *P_d, int nprob, const long long *off_d, const int *flag_d,
+                    const double *buf_d, cudaStream_t s) {
+    prof_begin(s);
+    k_scatter<<<nprob, 256, 0, s>>>(P_d, off_d, flag_d, buf_d);
+    prof_end(KC_AUX, s);
+    launch_counter() += 1;
+}
+
 void launch_restart(const Problem *P_d, int nprob, int, cudaStream_t s) {
+    prof_begin(s);
     k_restart<<<nprob, RTPB, 0, s>>>(P_d);
+    prof_end(KC_AUX, s);
     launch_counter() += 1;
 }
 
@@ -605,7 +657,9 @@ static void basis_t(const Problem *P_d, const Tile *tiles_d, int ntiles, int max
         cudaFuncSetAttribute(k_basis<MAXOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
         attr = true;
     }
+    prof_begin(s);
     k_basis<MAXOUT><<<ntiles, TPB, smem, s>>>(P_d, tiles_d);
+    prof_end(KC_BASIS, s);
 }
 
 void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, int max_nev,
@@ -620,7 +674,9 @@ void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_n
 }
 
 void launch_finalize(const Problem *P_d, int nprob, int, cudaStream_t s) {
+    prof_begin(s);
     k_finalize<<<nprob, RTPB, 0, s>>>(P_d);
+    prof_end(KC_AUX, s);
     launch_counter() += 1;
 }
 
@@ -631,7 +687,9 @@ void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_nc
         cudaFuncSetAttribute(k_ritz, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
         attr = true;
     }
+    prof_begin(s);
     k_ritz<<<ntiles, TPB, smem, s>>>(P_d, tiles_d);
+    prof_end(KC_RITZ, s);
     launch_counter() += 1;
 }
 

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(TPB) k_norm_init(const Problem *__restrict__ p
     __shared__ double scratch[32], mine[1], tot[1];
     double s = 0.0;
     for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) s = fma(P.r0[r], P.r0[r], s);
-    s = block_sum(s, scratch);
+    s = block_sum0(s, scratch);
     if (threadIdx.x == 0) mine[0] = s;
     __syncthreads();
     if (!finish_tile(P, blockIdx.x - P.tile0, 1, mine, tot)) return;
@@ -198,12 +198,14 @@ __global__ void __launch_bounds__(TPB) k_proj(const Problem *__restrict__ probs,
         }
     }
     __shared__ double red[MAXNCV + 1], tot[MAXNCV + 1];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        const int k = warp + 8 * i;
-        if (k < c) {
-            const double v = warp_sum(acc[i]);
-            if (lane == 0) red[k] = v;
+    {
+        const double v0 = warp_reduce8(acc);          // columns warp + 8 * (lane >> 2)
+        const int k0 = warp + 8 * (lane >> 2);
+        if ((lane & 3) == 0 && k0 < c) red[k0] = v0;
+        if (c > 64) {                                 // warp-uniform
+            const double v1 = warp_reduce8(acc + 8);
+            const int k1 = warp + 8 * (8 + (lane >> 2));
+            if ((lane & 3) == 0 && k1 < c) red[k1] = v1;
         }
     }
     if (pass == 1 && warp == 0) {
@@ -263,7 +265,7 @@ __global__ void __launch_bounds__(TPB) k_apply(const Problem *__restrict__ probs
         w[r] = acc;
         nrm = fma(acc, acc, nrm);
     }
-    nrm = block_sum(nrm, scratch);
+    nrm = block_sum0(nrm, scratch);
     if (threadIdx.x == 0) mine[0] = nrm;
     __syncthreads();
     if (!finish_tile(P, blockIdx.x - P.tile0, 1, mine, tot)) return;
@@ -386,23 +388,31 @@ __global__ void k_residuals_final(const double *__restrict__ part, int nblk, int
 void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, int prob,
                          unsigned long long seed, cudaStream_t s) {
     const unsigned long long key = sm_mix(seed * 0xD1B54A32D192ED03ULL + 0ULL);
+    prof_begin(s);
     k_start<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, prob, key);
+    prof_end(KC_AUX, s);
     launch_counter() += 1;
 }
 
 void launch_norm_init(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s) {
+    prof_begin(s);
     k_norm_init<<<ntiles, TPB, 0, s>>>(P_d, tiles_d);
+    prof_end(KC_AUX, s);
     launch_counter() += 1;
 }
 
 void launch_prep_f32(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, cudaStream_t s) {
+    prof_begin(s);
     k_prep<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, 0, nullptr);
+    prof_end(KC_SPMV, s);
     launch_counter() += 1;
 }
 
 void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, double *xout,
                      cudaStream_t s) {
+    prof_begin(s);
     k_prep<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, 1, xout);
+    prof_end(KC_AUX, s);
     launch_counter() += 1;
 }
 
@@ -412,16 +422,26 @@ void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, 
                  bool external_w, cudaStream_t s) {
     if (!external_w) {
         if (fp32_any) {
+            prof_begin(s);
             k_prep<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, 0, nullptr);
+            prof_end(KC_SPMV, s);
+            prof_begin(s);
             k_spmv_step<true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step);
+            prof_end(KC_SPMV, s);
             launch_counter() += 2;
         }
+        prof_begin(s);
         k_spmv_step<false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step);
+        prof_end(KC_SPMV, s);
         launch_counter() += 1;
     }
     for (int pass = 1; pass <= 3; ++pass) {
+        prof_begin(s);
         k_proj<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+        prof_end(KC_PROJ, s);
+        prof_begin(s);
         k_apply<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+        prof_end(KC_APPLY, s);
     }
     launch_counter() += 6;
 }

@@ -98,11 +98,13 @@ typedef struct {
     unsigned long long seed;  /* start-vector seed (SplitMix64 stream 0); default 0 */
     const double *start;      /* optional host start vector of length n (overrides seed) */
     void *stream;             /* cudaStream_t to run on; NULL = library-owned stream */
-    int use_graphs;           /* capture restart cycles as CUDA graphs (default 1 when 0 passed? see below) */
-    int reserved[7];
+    int use_graphs;           /* replay identical restart cycles as CUDA graphs */
+    int restart_on_device;    /* run the O(ncv^2) restart math in a device kernel instead of on the host */
+    int profile;              /* time every kernel launch with CUDA events (eager launches); see hlanc_last_profile */
+    int reserved[5];
 } hlanc_opts_t;
 
-/* Fill defaults (tol 0, max_restarts 200, FP64, seed 0, graphs on). */
+/* Fill defaults (tol 0, max_restarts 200, FP64, seed 0, graphs on, host restart). */
 void hlanc_opts_default(hlanc_opts_t *opts);
 
 typedef struct {
@@ -181,6 +183,20 @@ int hlanc_server_destroy(hlanc_server_t s);
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Number of kernels this library launched since load (all devices). */
 long long hlanc_kernel_launches(void);
+
+/* Per-kernel-class timing of the last solve run with opts.profile = 1 on the
+ * calling thread.  Classes: 0 SpMV, 1 CGS projection, 2 CGS update,
+ * 3 basis update (V*Q), 4 Ritz vectors, 5 auxiliary kernels, 6 host restart
+ * (CPU time).  bytes / flops are the algorithmic DRAM bytes and FP64 flops
+ * of the launches that did work. */
+#define HLANC_PROF_CLASSES 7
+typedef struct {
+    long long launches[HLANC_PROF_CLASSES];
+    double ms[HLANC_PROF_CLASSES];
+    double bytes[HLANC_PROF_CLASSES];
+    double flops[HLANC_PROF_CLASSES];
+} hlanc_profile_t;
+int hlanc_last_profile(hlanc_profile_t *out);
 
 #ifdef __cplusplus
 }
