@@ -1,0 +1,337 @@
+#!/usr/bin/env python
+"""Benchmark of the implicitly restarted Lanczos solver on one GB300.
+
+One step = one complete eigen-solve (start vector to converged Ritz pairs)
+of the workload.  Default workload: 3-D 7-point Dirichlet Laplacian on a
+160^3 grid (n = 4,096,000, nnz = 28,518,400) plus a diagonal shift
+uniform[0, 0.1) per row from seed 1, CSR int32/FP64, nev = 20, ncv = 60,
+largest algebraic, tolerance 1e-10, start vector uniform[-1, 1) from seed 0.
+Metric: converged eigenpairs per second; a step counts only if every
+returned pair has ||A v - lambda v|| <= 1e-10 ||A||_inf.
+
+    value   device-resident: CSR already in HBM, outputs to device buffers,
+            CUDA events on the solver's stream around K solves
+    e2e     through the C ABI with host buffers: dcsrmv_operator_gpu
+            construction (CSR host->device) + ds_solver_gpu writing host
+            values/vectors (+ operator teardown), wall clock per solve
+    roofline  the dominant kernel class of one profiled solve (CUDA events
+            around every launch): algorithmic bytes / time vs the measured
+            HBM peak, and FP64 flops / time vs the live FP64 probe
+
+`--impl reference` times the oracle's C restatement of the reference CPU
+solver (oracle/, OpenMP over all host cores) on the same workload: each step
+is one restart cycle's worth of Lanczos steps, extrapolated to the SpMV
+count of the full solve.  Multi-GPU runs are independent replicas (the
+reference path does not shard a solve): value sums every rank's rate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from hlanc_gb300 import generators as G  # noqa: E402
+
+# SpMV calls of a full solve of each workload, measured with this library on
+# GB300 (the algorithm's count; the CPU baseline extrapolates its sampled
+# per-step time with it).
+WORKLOADS = {
+    "lap3d_160": dict(desc="3-D Laplacian 160^3 + U[0,0.1) diagonal shift (seed 1)",
+                      gen=lambda: G.laplacian_3d(160, shift_seed=1), nev=20, ncv=60, tol=1e-10),
+    "lap3d_100": dict(desc="3-D Laplacian 100^3 + U[0,0.1) diagonal shift (seed 1)",
+                      gen=lambda: G.laplacian_3d(100, shift_seed=1), nev=20, ncv=60, tol=1e-10),
+    "lap3d_64": dict(desc="3-D Laplacian 64^3 + U[0,0.1) diagonal shift (seed 1)",
+                     gen=lambda: G.laplacian_3d(64, shift_seed=1), nev=20, ncv=60, tol=1e-10),
+    "lap2d_100": dict(desc="2-D Laplacian 100^2 (reference tolerance dlamch('E'))",
+                      gen=lambda: G.laplacian_2d(100), nev=10, ncv=30, tol=0.0),
+}
+FULL_SOLVE_SPMV = {"lap3d_160": 3460, "lap3d_100": None, "lap3d_64": 1312, "lap2d_100": 1375}
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:  # noqa: BLE001
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def read_traffic(kernel_class: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/*.txt line 'traffic_per_launch_bytes <class> <value>')."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith(".txt"):
+            continue
+        with open(os.path.join(d, fn)) as f:
+            for line in f:
+                p = line.split()
+                if len(p) == 3 and p[0] == "traffic_per_launch_bytes" and p[1] == kernel_class:
+                    return float(p[2])
+    return None
+
+
+def dist_setup(ngpus):
+    rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
+    local = _env_int("LOCAL_RANK", 0)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(m, wl, threads, full_spmv):
+    """Oracle port, first restart cycle of the same solve; extrapolated."""
+    import oracle
+    oracle.build()
+    x0 = G.start_vector(m.n, 0)
+    t = time.perf_counter()
+    rc, vals, vecs, st = oracle.solve_csr(m.row_ptr, m.col, m.val, m.ncols, False, wl["nev"], wl["ncv"], x0,
+                                          tol=wl["tol"], max_iter=1, threads=threads)
+    dt = time.perf_counter() - t
+    per_spmv = dt / max(st["spmv_calls"], 1)
+    est = per_spmv * full_spmv
+    return dict(value=wl["nev"] / est, unit="eigenpairs/s", cores=threads, kind="port",
+                sample=(f"first restart cycle ({st['spmv_calls']} Lanczos steps, {dt:.2f} s) of the same solve "
+                        f"on {threads} threads, extrapolated to the full solve's {full_spmv} SpMV steps"),
+                seconds_per_step=per_spmv)
+
+
+def run_reference(args, wl, m):
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    full = FULL_SOLVE_SPMV.get(args.workload) or args.full_spmv
+    for _ in range(args.warmup):
+        cpu_sample(m, wl, threads, full)
+    vals = [cpu_sample(m, wl, threads, full) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    secs = wl["nev"] / v
+    line = {"metric": "converged eigenpairs/s (resid <= 1e-10 ||A||)", "value": v, "unit": "eigenpairs/s",
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded generator)",
+            "config": config_of(args, wl, m),
+            "cpu_baseline": {"value": v, "unit": "eigenpairs/s", "cores": threads, "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args, wl, m):
+    return {"workload": args.workload, "description": wl["desc"], "n": m.n, "nnz": m.nnz, "nev": wl["nev"],
+            "ncv": wl["ncv"], "tol": wl["tol"] or "dlamch(E)", "which": "largest algebraic",
+            "start": "uniform[-1,1) seed 0", "precision": "fp64",
+            "l2": "inputs larger than L2 (CSR + basis >> 129 MB); no flush needed",
+            "parallelism": "replicas"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="lap3d_160", choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--full-spmv", type=int, default=0, help="SpMV count of a full solve (CPU extrapolation)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    m = wl["gen"]()
+    if args.impl == "reference":
+        run_reference(args, wl, m)
+        return
+
+    import torch
+
+    import hlanc_gb300 as H
+    from hlanc_gb300 import build
+    rank, world, local, pg = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    build.build()
+    dev = local
+    nev, ncv, tol = wl["nev"], wl["ncv"], wl["tol"]
+    op = H.dcsrmv_operator_gpu(m, dev=dev)
+    stream = torch.cuda.Stream()
+    vals = torch.zeros(ncv, dtype=torch.float64, device="cuda")
+    vecs = torch.zeros((ncv, m.n), dtype=torch.float64, device="cuda")
+    norm_a = float(np.abs(G.to_scipy(m)).sum(axis=1).max())
+
+    def solve_dev(**kw):
+        return H.solve_device(op, nev, ncv, vals.data_ptr(), vecs.data_ptr(), m.n, dev=dev, tol=tol,
+                              stream=stream.cuda_stream, **kw)
+
+    for _ in range(args.warmup):
+        st = solve_dev()
+    torch.cuda.synchronize()
+    barrier(pg)
+    launches0 = H.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            stats.append(solve_dev())
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = H.kernel_launches() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = allmax(pg, ms)
+    barrier(pg)
+    res, rdiff = H.residuals_device(op, nev, vals.data_ptr(), vecs.data_ptr(), m.n)
+    valid = all(s["rc"] == 0 and s["nconv"] >= nev for s in stats) and float(res.max()) <= 1e-10 * norm_a
+    value = world * nev / (ms / 1e3) if valid else 0.0
+
+    # end to end through the C ABI with host buffers
+    values_h = np.zeros(ncv)
+    vectors_h = np.zeros((m.n, ncv), order="F")
+    e2e_ms = []
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        op2 = H.dcsrmv_operator_gpu(m, dev=dev)
+        st2: dict = {}
+        rc = H.ds_solver_gpu(m.n, nev, ncv, values_h, vectors_h, m.n, op2, dev, opts_=H.opts(tol=tol), stats=st2)
+        op2.close()
+        e2e_ms.append((time.perf_counter() - t) * 1e3)
+        valid = valid and rc == 0
+    e2e_ms = allmax(pg, statistics.median(e2e_ms))
+    h2d = 4 * (m.n + 1) + 12 * m.nnz
+    d2h = 8 * nev + 8 * m.n * ncv
+
+    # roofline: one profiled solve
+    pst = solve_dev(profile=True)
+    prof = H.last_profile()
+    kernel_classes = ["spmv", "cgs_proj", "cgs_apply", "basis", "ritz"]
+    dom = max(kernel_classes, key=lambda k: prof[k]["ms"])
+    total_kernel_ms = sum(prof[k]["ms"] for k in kernel_classes + ["aux"])
+    peak, peak_src = measured_peaks()
+    fp64_peak = H.fp64_peak_tflops(dev)
+    d = prof[dom]
+    achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9 if d["ms"] else 0.0
+    traffic = read_traffic(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic": traffic,
+                "bytes_per_launch": d["bytes"] / max(d["launches"], 1),
+                "avg_launch_ms": d["ms"] / max(d["launches"], 1),
+                "fp64": {"achieved_tflops": d["flops"] / (d["ms"] * 1e-3) / 1e12 if d["ms"] else 0.0,
+                         "peak_tflops": fp64_peak, "frac": (d["flops"] / (d["ms"] * 1e-3) / 1e12) / fp64_peak
+                         if d["ms"] else 0.0, "peak_source": "measured live (hlanc_diag_fp64_tflops)"},
+                "time_share": {k: prof[k]["ms"] / total_kernel_ms for k in kernel_classes + ["aux"]},
+                "host_restart_ms": prof["host_restart"]["ms"]}
+    line = {"metric": "converged eigenpairs/s (resid <= 1e-10 ||A||)", "value": value, "unit": "eigenpairs/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generator)", "config": config_of(args, wl, m),
+            "valid": bool(valid), "max_residual_over_normA": float(res.max()) / norm_a,
+            "solve": {"spmv_calls": stats[-1]["spmv_calls"], "restarts": stats[-1]["restarts"],
+                      "cgs_passes": stats[-1]["cgs_passes"], "nconv": stats[-1]["nconv"]},
+            "e2e": {"value": world * nev / (e2e_ms / 1e3) if valid else 0.0, "unit": "eigenpairs/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "roofline": roofline, "gpu_launches": launches, "clocks": clk.summary()}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        full = FULL_SOLVE_SPMV.get(args.workload) or stats[-1]["spmv_calls"]
+        line["cpu_baseline"] = cpu_sample(m, wl, os.cpu_count() or 1, full)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

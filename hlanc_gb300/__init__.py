@@ -103,6 +103,7 @@ def _declare(L):
         "hlanc_solve_device": (_i, [_i, _i, _i, _i, _p, _p, _i, _p, C.POINTER(Opts), C.POINTER(Stats)]),
         "hlanc_residuals_device": (_i, [_p, _i, _p, _p, _i, _p, _p]),
         "hlanc_last_profile": (_i, [C.POINTER(Profile)]),
+        "hlanc_diag_fp64_tflops": (_i, [_i, C.POINTER(C.c_double)]),
         "hlanc_batch_create": (_i, [_i, _i, _p, _p, _p, C.POINTER(Opts), C.POINTER(_p)]),
         "hlanc_batch_run": (_i, [_p, _p, _p, _p, C.POINTER(Stats)]),
         "hlanc_batch_destroy": (_i, [_p]),
@@ -349,6 +350,13 @@ def residuals_device(op: dcsrmv_operator_gpu, k: int, values_ptr: int, vectors_p
 
 def kernel_launches() -> int:
     return int(lib().hlanc_kernel_launches())
+
+
+def fp64_peak_tflops(dev: int = 0) -> float:
+    """Measured FP64 FMA throughput of the device (TFLOP/s)."""
+    t = C.c_double()
+    _check(lib().hlanc_diag_fp64_tflops(dev, C.byref(t)), "fp64 probe")
+    return t.value
 
 
 def last_profile() -> dict:

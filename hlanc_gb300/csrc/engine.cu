@@ -408,12 +408,11 @@ public:
         return HLANC_OK;
     }
 
+    // graph key for the basis kernel instantiation launch_basis picks
     static int basis_bucket(int nev) {
         if (nev <= 0) return 0;
-        const int b[] = {8, 16, 24, 32, 48, 64};
-        for (int x : b)
-            if (nev <= x) return x;
-        return 64;
+        const int q = (nev + 3) / 4;
+        return q <= 10 ? 4 * q : q <= 12 ? 48 : q <= 14 ? 56 : 64;
     }
 
     // Device part of one cycle: apply pending restarts, extend, (restart), gather.
@@ -435,11 +434,15 @@ public:
         return HLANC_OK;
     }
 
-    int pull_mailbox() {
+    // Copy the gathered State/h of the active problems into their host
+    // mirrors; with `only`, just those problems (a finalisation must not
+    // overwrite the restart decisions of problems still running).
+    int pull_mailbox(const std::vector<int> *only = nullptr) {
         CK(cudaMemcpyAsync(mbox_h, mbox_d, sizeof(double) * mbox_used, cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
         for (size_t a = 0; a < active.size(); ++a) {
+            if (only && std::find(only->begin(), only->end(), active[a]) == only->end()) continue;
             ProbRes &p = probs[active[a]];
             const double *slot = mbox_h + off_h[a];
             memcpy(&p.hs, slot, sizeof(State));
@@ -607,7 +610,7 @@ public:
         launch_gather(P_d, (int)active.size(), off_d, mbox_d, stream);
         CK(cudaGetLastError());
         for (size_t q = 0; q < active.size(); ++q) flag_h[q] = 0;
-        return pull_mailbox();
+        return pull_mailbox(&which);
     }
     int finalize(int prob) { return finalize_many(std::vector<int>{prob}); }
 

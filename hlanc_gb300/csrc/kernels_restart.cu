@@ -662,14 +662,25 @@ static void basis_t(const Problem *P_d, const Tile *tiles_d, int ntiles, int max
     prof_end(KC_BASIS, s);
 }
 
+// nev is rounded up to a multiple of 4: the unrolled output loop issues no
+// FP64 instruction for more than 3 absent columns.
 void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, int max_nev,
                   cudaStream_t s) {
-    if (max_nev <= 8) basis_t<8>(P_d, tiles_d, ntiles, max_ncv, s);
-    else if (max_nev <= 16) basis_t<16>(P_d, tiles_d, ntiles, max_ncv, s);
-    else if (max_nev <= 24) basis_t<24>(P_d, tiles_d, ntiles, max_ncv, s);
-    else if (max_nev <= 32) basis_t<32>(P_d, tiles_d, ntiles, max_ncv, s);
-    else if (max_nev <= 48) basis_t<48>(P_d, tiles_d, ntiles, max_ncv, s);
-    else basis_t<64>(P_d, tiles_d, ntiles, max_ncv, s);
+    switch ((max_nev + 3) / 4) {
+    case 0: case 1: basis_t<4>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 2: basis_t<8>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 3: basis_t<12>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 4: basis_t<16>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 5: basis_t<20>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 6: basis_t<24>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 7: basis_t<28>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 8: basis_t<32>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 9: basis_t<36>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 10: basis_t<40>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 11: case 12: basis_t<48>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    case 13: case 14: basis_t<56>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    default: basis_t<64>(P_d, tiles_d, ntiles, max_ncv, s); break;
+    }
     launch_counter() += 1;
 }
 

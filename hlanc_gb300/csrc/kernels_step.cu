@@ -160,9 +160,53 @@ __global__ void __launch_bounds__(TPB) k_prep(const Problem *__restrict__ probs,
 }
 
 // ---- CGS projection: h = V[:, 0:c)^T w  (+ ||w||^2 on pass 1) ----------------
-// Warp w owns columns k = w, w+8, ...; lane l owns rows l and l+32 of every
-// 64-row chunk.  Accumulators stay in registers for the whole tile.
-__global__ void __launch_bounds__(TPB) k_proj(const Problem *__restrict__ probs,
+// Warp w owns columns k = w + 8 i (i < CPW = ceil(c / 8)); lane l owns rows
+// l and l+32 of every 64-row chunk, so every V load is a coalesced 256-byte
+// warp access.  The column count per warp is a template parameter picked on
+// the device from c: no FP64 instruction is issued for a column that does
+// not exist (predicated-off FP64 instructions still occupy GB300's FP64
+// pipe).  Accumulators stay in registers for the whole tile; one transposed
+// shuffle reduction per 8 columns ends the tile.
+template <int CPW>
+__device__ __forceinline__ void proj_tile(const Problem &P, const Tile &t, const double *__restrict__ w, int c0,
+                                          int cc, bool with_norm, double *red) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t ld = (size_t)P.ld;
+    double acc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = 0.0;
+    double nrm = 0.0;
+    const bool last_full = warp + 8 * (CPW - 1) < cc;    // warp-uniform
+    for (int r = t.row0; r < t.row1; r += 64) {
+        const double w0 = w[r + lane];
+        const double w1 = w[r + 32 + lane];
+        if (with_norm && warp == 0) {
+            nrm = fma(w0, w0, nrm);
+            nrm = fma(w1, w1, nrm);
+        }
+        const double *__restrict__ vb = P.V + r + lane + (size_t)(c0 + warp) * ld;
+#pragma unroll
+        for (int i = 0; i < CPW - 1; ++i) {
+            const double *vk = vb + (size_t)(8 * i) * ld;
+            acc[i] = fma(__ldcs(vk), w0, acc[i]);
+            acc[i] = fma(__ldcs(vk + 32), w1, acc[i]);
+        }
+        if (last_full) {
+            const double *vk = vb + (size_t)(8 * (CPW - 1)) * ld;
+            acc[CPW - 1] = fma(__ldcs(vk), w0, acc[CPW - 1]);
+            acc[CPW - 1] = fma(__ldcs(vk + 32), w1, acc[CPW - 1]);
+        }
+    }
+    const double v = warp_reduce8(acc);                  // column c0 + warp + 8 * (lane >> 2)
+    const int k = warp + 8 * (lane >> 2);
+    if ((lane & 3) == 0 && k < cc) red[c0 + k] = v;
+    if (with_norm && warp == 0) {
+        nrm = warp_sum(nrm);
+        if (lane == 0) red[c0 + cc] = nrm;
+    }
+}
+
+__global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ probs,
                                               const Tile *__restrict__ tiles, int s, int pass) {
     const Tile t = tiles[blockIdx.x];
     const Problem &P = probs[t.prob];
@@ -172,45 +216,22 @@ __global__ void __launch_bounds__(TPB) k_proj(const Problem *__restrict__ probs,
     const int j = S->k + s;
     const int c = j + 1;
     const int m = P.ncv;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const double *__restrict__ w = step_out(P, j);
-    const size_t ld = (size_t)P.ld;
-    double acc[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) acc[i] = 0.0;
-    double nrm = 0.0;
-    for (int r = t.row0; r < t.row1; r += 64) {
-        const double w0 = w[r + lane];
-        const double w1 = w[r + 32 + lane];
-        if (pass == 1 && warp == 0) {
-            nrm = fma(w0, w0, nrm);
-            nrm = fma(w1, w1, nrm);
-        }
-        const double *__restrict__ vb = P.V + r + lane;
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            const int k = warp + 8 * i;
-            if (k < c) {
-                const double *vk = vb + (size_t)k * ld;
-                acc[i] = fma(__ldcs(vk), w0, acc[i]);
-                acc[i] = fma(__ldcs(vk + 32), w1, acc[i]);
-            }
-        }
-    }
     __shared__ double red[MAXNCV + 1], tot[MAXNCV + 1];
-    {
-        const double v0 = warp_reduce8(acc);          // columns warp + 8 * (lane >> 2)
-        const int k0 = warp + 8 * (lane >> 2);
-        if ((lane & 3) == 0 && k0 < c) red[k0] = v0;
-        if (c > 64) {                                 // warp-uniform
-            const double v1 = warp_reduce8(acc + 8);
-            const int k1 = warp + 8 * (8 + (lane >> 2));
-            if ((lane & 3) == 0 && k1 < c) red[k1] = v1;
+    // panels of up to 64 columns (8 per warp); the norm rides on the last panel
+    for (int c0 = 0; c0 < c; c0 += 64) {
+        const int cc = min(64, c - c0);
+        const bool nrm = pass == 1 && c0 + cc == c;
+        switch ((cc + 7) >> 3) {
+        case 1: proj_tile<1>(P, t, w, c0, cc, nrm, red); break;
+        case 2: proj_tile<2>(P, t, w, c0, cc, nrm, red); break;
+        case 3: proj_tile<3>(P, t, w, c0, cc, nrm, red); break;
+        case 4: proj_tile<4>(P, t, w, c0, cc, nrm, red); break;
+        case 5: proj_tile<5>(P, t, w, c0, cc, nrm, red); break;
+        case 6: proj_tile<6>(P, t, w, c0, cc, nrm, red); break;
+        case 7: proj_tile<7>(P, t, w, c0, cc, nrm, red); break;
+        default: proj_tile<8>(P, t, w, c0, cc, nrm, red); break;
         }
-    }
-    if (pass == 1 && warp == 0) {
-        nrm = warp_sum(nrm);
-        if (lane == 0) red[c] = nrm;
     }
     __syncthreads();
     if (!finish_tile(P, blockIdx.x - P.tile0, c + (pass == 1 ? 1 : 0), red, tot)) return;
@@ -231,7 +252,7 @@ __global__ void __launch_bounds__(TPB) k_proj(const Problem *__restrict__ probs,
 }
 
 // ---- CGS update: w -= V[:, 0:c) h ; DGKS decision ------------------------------
-__global__ void __launch_bounds__(TPB) k_apply(const Problem *__restrict__ probs,
+__global__ void __launch_bounds__(TPB, 6) k_apply(const Problem *__restrict__ probs,
                                                const Tile *__restrict__ tiles, int s, int pass) {
     const Tile t = tiles[blockIdx.x];
     const Problem &P = probs[t.prob];

@@ -198,6 +198,10 @@ typedef struct {
 } hlanc_profile_t;
 int hlanc_last_profile(hlanc_profile_t *out);
 
+/* Measured dense FP64 FMA throughput of device `dev` (TFLOP/s): the ceiling
+ * of kernels that issue one FP64 FMA per loaded 8-byte element. */
+int hlanc_diag_fp64_tflops(int dev, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif
