@@ -129,9 +129,11 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def read_traffic(kernel_class: str):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/*.txt line 'traffic_per_launch_bytes <class> <value>')."""
+def read_traffic_ratio(kernel_class: str):
+    """DRAM bytes / algorithmic bytes of a kernel class from the committed ncu
+    summary (profiles/*.txt line 'traffic_ratio_dram_over_algorithmic <class> <r>');
+    the traffic of a launch here is that ratio times its algorithmic bytes
+    (traffic grows in proportion to the rows and columns a launch streams)."""
     d = os.path.join(ROOT, "profiles")
     if not os.path.isdir(d):
         return None
@@ -141,7 +143,7 @@ def read_traffic(kernel_class: str):
         with open(os.path.join(d, fn)) as f:
             for line in f:
                 p = line.split()
-                if len(p) == 3 and p[0] == "traffic_per_launch_bytes" and p[1] == kernel_class:
+                if len(p) == 3 and p[0] == "traffic_ratio_dram_over_algorithmic" and p[1] == kernel_class:
                     return float(p[2])
     return None
 
@@ -303,10 +305,12 @@ def main():
     fp64_peak = H.fp64_peak_tflops(dev)
     d = prof[dom]
     achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9 if d["ms"] else 0.0
-    traffic = read_traffic(dom)
+    ratio = read_traffic_ratio(dom)
+    traffic = ratio * d["bytes"] / max(d["launches"], 1) if ratio else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                "traffic": traffic,
+                "traffic": traffic, "traffic_source": "ncu dram bytes / algorithmic bytes (profiles/) x "
+                                                          "algorithmic bytes per launch" if ratio else None,
                 "bytes_per_launch": d["bytes"] / max(d["launches"], 1),
                 "avg_launch_ms": d["ms"] / max(d["launches"], 1),
                 "fp64": {"achieved_tflops": d["flops"] / (d["ms"] * 1e-3) / 1e12 if d["ms"] else 0.0,
