@@ -1002,6 +1002,17 @@ int hlanc_csr_info(hlanc_csr_t h, int *dev, int *nrows, int *ncols, long long *n
     return HLANC_OK;
 }
 
+}  // extern "C"
+
+int hlanc::csr_view_of(hlanc_csr_t h, hlanc::CsrView *out) {
+    if (!h || !out) return HLANC_ERR_INVALID;
+    out->dev = h->dev; out->nrows = h->nrows; out->ncols = h->ncols; out->nnz = h->nnz;
+    out->rp_d = h->rp_d; out->ci_d = h->ci_d; out->val_d = h->val_d; out->stream = h->stream;
+    return HLANC_OK;
+}
+
+extern "C" {
+
 static bool is_device_ptr(const void *p, int dev) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {

@@ -235,4 +235,14 @@ void launch_residuals(const int *row_ptr, const int *col, const double *val, int
 
 long long &launch_counter();
 
+// Read-only view of a device CSR operator's arrays (engine.cu).
+struct CsrView {
+    int dev, nrows, ncols;
+    long long nnz;
+    const int *rp_d, *ci_d;
+    const double *val_d;
+    cudaStream_t stream;
+};
+int csr_view_of(hlanc_csr_t csr, CsrView *out);
+
 }  // namespace hlanc

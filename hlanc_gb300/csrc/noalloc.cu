@@ -1,0 +1,143 @@
+// noalloc.cu -- residual verifier that allocates no memory.
+//
+// hlanc_residuals_device (engine.cu) allocates its partial-sum buffers on
+// every call.  Some callers cannot allocate device memory at that point: a
+// serving process whose HBM pool is already fully claimed by its own
+// allocator, or a monitoring loop that checks Ritz pairs between solves and
+// must not pay (or wait on) a cudaMalloc/cudaFree.  This file gives them one
+// entry point with the same result whose scratch lives in a file-scope
+// __device__ array of fixed size: HLANC_NOALLOC_MAX_PAIRS pairs.
+//
+// Every GPU that loads the library keeps this array (about 513 KB) until the
+// process exits.  All calls share it, and it keeps the last call's contents:
+// every slot a call reads is written earlier in the same call, so nothing has
+// to start at zero, but calls that overlap on the GPU (from several host
+// threads or streams) race on the array and must be serialised by the caller.
+//
+// Host code cannot use the array's name as a device address (there it is a
+// host-side stand-in), so the first call on each device looks the address up
+// with cudaGetSymbolAddress, with that device current, and caches it; make
+// that first call outside any stream capture.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "internal.cuh"
+
+namespace {
+
+constexpr int NA_BLOCKS = 256;                       // CTAs per pair
+constexpr int NA_MAX = HLANC_NOALLOC_MAX_PAIRS;      // pairs per call
+constexpr int NA_PART = NA_MAX * NA_BLOCKS * 4;      // per-CTA partials
+constexpr int NA_TOTAL = NA_PART + 2 * NA_MAX;       // + resid / rdiff results
+
+static __device__ __align__(256) double g_noalloc_scratch[NA_TOTAL];
+
+constexpr int NA_MAX_DEVICES = 64;
+std::mutex g_na_mu;
+double *g_na_ptr[NA_MAX_DEVICES] = {nullptr};
+
+// Per CTA of pair i: sum of squares of A v - lambda v, max |A v - lambda v|,
+// max |A v|, max |lambda v| over its rows (the quantities of verify_eigs).
+__global__ void __launch_bounds__(256) k_na_resid_part(const int *__restrict__ rp, const int *__restrict__ ci,
+                                                       const double *__restrict__ val, int n,
+                                                       const double *__restrict__ values,
+                                                       const double *__restrict__ V, int ldv,
+                                                       double *__restrict__ scratch) {
+    const int i = blockIdx.y;
+    const double lam = values[i];
+    const double *v = V + (size_t)i * ldv;
+    double ss = 0.0, md = 0.0, ma = 0.0, mb = 0.0;
+    for (int r = blockIdx.x * 256 + threadIdx.x; r < n; r += gridDim.x * 256) {
+        double acc = 0.0;
+        for (int q = rp[r]; q < rp[r + 1]; ++q) acc = fma(val[q], v[ci[q]], acc);
+        const double lv = lam * v[r];
+        const double d = acc - lv;
+        ss = fma(d, d, ss);
+        md = fmax(md, fabs(d));
+        ma = fmax(ma, fabs(acc));
+        mb = fmax(mb, fabs(lv));
+    }
+    __shared__ double sh[4][8];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        md = fmax(md, __shfl_xor_sync(0xffffffffu, md, o));
+        ma = fmax(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+        mb = fmax(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+    }
+    if (lane == 0) { sh[0][warp] = ss; sh[1][warp] = md; sh[2][warp] = ma; sh[3][warp] = mb; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0, c = 0, d = 0;
+        for (int w = 0; w < 8; ++w) { a += sh[0][w]; b = fmax(b, sh[1][w]); c = fmax(c, sh[2][w]); d = fmax(d, sh[3][w]); }
+        double *o = scratch + ((size_t)i * gridDim.x + blockIdx.x) * 4;
+        o[0] = a; o[1] = b; o[2] = c; o[3] = d;
+    }
+}
+
+// resid[i] = sqrt(sum), rdiff[i] = max|d| / max(max|Av|, max|lambda v|).
+__global__ void k_na_resid_final(int nblk, int k, double *__restrict__ scratch) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    double a = 0, b = 0, c = 0, d = 0;
+    for (int q = 0; q < nblk; ++q) {
+        const double *o = scratch + ((size_t)i * nblk + q) * 4;
+        a += o[0]; b = fmax(b, o[1]); c = fmax(c, o[2]); d = fmax(d, o[3]);
+    }
+    const double mx = fmax(c, d);
+    scratch[NA_PART + i] = sqrt(a);
+    scratch[NA_PART + NA_MAX + i] = mx > 0.0 ? b / mx : b;
+}
+
+// Device address of the scratch array on `dev` (looked up once per device).
+int scratch_for(int dev, double **out) {
+    if (dev < 0 || dev >= NA_MAX_DEVICES) return HLANC_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_ptr[dev]) {
+        int prev = -1;
+        if (cudaGetDevice(&prev) != cudaSuccess) return HLANC_ERR_CUDA;
+        if (prev != dev && cudaSetDevice(dev) != cudaSuccess) return HLANC_ERR_CUDA;
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (prev != dev) cudaSetDevice(prev);
+        if (e != cudaSuccess || !p) return HLANC_ERR_CUDA;
+        g_na_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_na_ptr[dev];
+    return HLANC_OK;
+}
+
+}  // namespace
+
+extern "C" int hlanc_residuals_device_noalloc(hlanc_csr_t csr, int k, const double *values_d,
+                                              const double *vectors_d, int ldv_d, double *resid_h,
+                                              double *rdiff_h) {
+    hlanc::CsrView c;
+    if (!csr || k <= 0 || !values_d || !vectors_d || !resid_h || !rdiff_h) return HLANC_ERR_INVALID;
+    if (hlanc::csr_view_of(csr, &c) != HLANC_OK || ldv_d < c.nrows || c.ncols > c.nrows) return HLANC_ERR_INVALID;
+    if (k > NA_MAX) return HLANC_ERR_UNSUPPORTED;   // more pairs than the fixed scratch holds
+    double *scratch = nullptr;
+    int rc = scratch_for(c.dev, &scratch);
+    if (rc) return rc;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != c.dev) cudaSetDevice(c.dev);
+    int nblk = (c.nrows + 255) / 256;
+    if (nblk > NA_BLOCKS) nblk = NA_BLOCKS;
+    if (nblk < 1) nblk = 1;
+    k_na_resid_part<<<dim3(nblk, k), 256, 0, c.stream>>>(c.rp_d, c.ci_d, c.val_d, c.nrows, values_d, vectors_d,
+                                                         ldv_d, scratch);
+    k_na_resid_final<<<(k + 127) / 128, 128, 0, c.stream>>>(nblk, k, scratch);
+    hlanc::launch_counter() += 2;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(resid_h, scratch + NA_PART, sizeof(double) * k, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(rdiff_h, scratch + NA_PART + NA_MAX, sizeof(double) * k, cudaMemcpyDeviceToHost,
+                            c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (prev != c.dev) cudaSetDevice(prev);
+    return e == cudaSuccess ? HLANC_OK : HLANC_ERR_CUDA;
+}

@@ -147,6 +147,22 @@ int hlanc_solve_device(int dev, int n, int nev, int ncv, double *values_d, doubl
 int hlanc_residuals_device(hlanc_csr_t csr, int k, const double *values_d,
                            const double *vectors_d, int ldv_d, double *resid_h, double *rdiff_h);
 
+/* Variant of hlanc_residuals_device that allocates nothing; it has no
+ * counterpart in the reference.  For callers that cannot allocate device
+ * memory when they verify Ritz pairs (a process whose HBM pool is already
+ * fully claimed by its own allocator, or a loop that must not wait on a
+ * cudaMalloc/cudaFree).  Its scratch is a fixed __device__ array of about
+ * 513 KB, held by every GPU that loads the library until exit; k may be at
+ * most HLANC_NOALLOC_MAX_PAIRS (larger k returns HLANC_ERR_UNSUPPORTED).
+ * resid_h / rdiff_h are host arrays of k doubles.  All calls share the
+ * scratch, so calls that overlap on the GPU race; serialise them.  The first
+ * call on a device looks up the scratch address, so make it outside any
+ * stream capture.  Synchronous. */
+#define HLANC_NOALLOC_MAX_PAIRS 64
+int hlanc_residuals_device_noalloc(hlanc_csr_t csr, int k, const double *values_d,
+                                   const double *vectors_d, int ldv_d, double *resid_h,
+                                   double *rdiff_h);
+
 /* ---- batched solves (one launch sequence over many problems) ----------- */
 typedef struct hlanc_batch_s *hlanc_batch_t;
 
