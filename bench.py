@@ -212,6 +212,166 @@ def run_reference(args, wl, m):
     print(json.dumps(line), flush=True)
 
 
+def batch_problems(count, seed=3):
+    """The batched workload: `count` symmetric banded-random matrices, n
+    log-uniform in [2000, 200000], half-bandwidth uniform in {2..16}, 10% of
+    rows with 1-8 extra off-band entries, N(0,1) entries, diagonal N(0, 4)."""
+    ns, bws = G.batched_problem_sizes(count, 2000, 200000, 2, 16, seed=seed)
+    return [G.banded_random(int(n), int(b), seed=seed, problem=i) for i, (n, b) in enumerate(zip(ns, bws))]
+
+
+def run_batch(args):
+    """Batched form vs the plain FP64 drop-in run one problem at a time."""
+    import torch
+
+    import hlanc_gb300 as H
+    from hlanc_gb300 import build
+    build.build()
+    mats = batch_problems(args.batch_count)
+    nev, ncv = 8, 24
+    out = {}
+    for mode, prec in (("fp64", H.HLANC_PREC_FP64), ("fp32_refine", H.HLANC_PREC_FP32_REFINE)):
+        ops = [H.dcsrmv_operator_gpu(m, precision=prec) for m in mats]
+        vals = [torch.zeros(ncv, dtype=torch.float64, device="cuda") for _ in mats]
+        vecs = [torch.zeros((ncv, m.n), dtype=torch.float64, device="cuda") for m in mats]
+        times = []
+        for rep in range(args.warmup + args.steps):
+            b = H.Batch(ops, nev, ncv, precision=prec, tol=1e-10)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            status, st = b.run([v.data_ptr() for v in vals], [x.data_ptr() for x in vecs])
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t
+            b.close()
+            if rep >= args.warmup:
+                times.append(dt)
+        ok = int((status == 0).sum())
+        worst = 0.0
+        for m, op, v, x in zip(mats, ops, vals, vecs):
+            r, _ = H.residuals_device(op, nev, v.data_ptr(), x.data_ptr(), m.n)
+            worst = max(worst, float(r.max()) / float(np.abs(G.to_scipy(m)).sum(axis=1).max()))
+        t = statistics.median(times)
+        out[f"batched_{mode}"] = {"seconds": t, "eigenpairs_per_s": ok * nev / t, "converged": ok,
+                                  "max_residual_over_normA": worst, "spmv_calls": st["spmv_calls"]}
+        if mode == "fp64":
+            # plain FP64 drop-in, one solve after another (same GPU, same problems)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            okp = 0
+            for m, op, v, x in zip(mats, ops, vals, vecs):
+                stp = H.solve_device(op, nev, ncv, v.data_ptr(), x.data_ptr(), m.n, tol=1e-10)
+                okp += stp["rc"] == 0
+            torch.cuda.synchronize()
+            tp = time.perf_counter() - t
+            out["plain_fp64_one_at_a_time"] = {"seconds": tp, "eigenpairs_per_s": okp * nev / tp, "converged": okp}
+        del ops
+    best = max(out["batched_fp64"]["eigenpairs_per_s"], out["batched_fp32_refine"]["eigenpairs_per_s"])
+    line = {"metric": "converged eigenpairs/s (resid <= 1e-10 ||A||), batched", "value":
+            out["batched_fp32_refine"]["eigenpairs_per_s"], "unit": "eigenpairs/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64 (fp32 SpMV)",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": f"batch{args.batch_count}", "nev": nev, "ncv": ncv, "tol": 1e-10,
+                       "matrices": "banded random, n log-uniform [2000,200000], half-bandwidth U{2..16}, seed 3"},
+            "results": out, "speedup_vs_plain_fp64": best / out["plain_fp64_one_at_a_time"]["eigenpairs_per_s"]}
+    print(json.dumps(line), flush=True)
+
+
+def serve_requests(count, seed=4, rate=200.0, n_lo=1000, n_hi=200000):
+    """Poisson request stream: exponential inter-arrival times (mean 1/rate)
+    from seed, n log-uniform in [n_lo, n_hi], generator uniform over the
+    workloads' families, nev uniform in {4, 8, 16}, ncv = 3 nev, 70% FP32-SpMV
+    + refinement and 30% plain FP64."""
+    u = G.uniform01(seed, 40, 6 * count).reshape(count, 6)
+    arrivals = np.cumsum(-np.log(1.0 - u[:, 0]) / rate)
+    reqs = []
+    for i in range(count):
+        n = int(np.exp(np.log(n_lo) + u[i, 1] * (np.log(n_hi) - np.log(n_lo))))
+        fam = int(u[i, 2] * 4)
+        if fam == 0:
+            nx = max(int(round(np.sqrt(n))), 8)
+            m = G.laplacian_2d(nx)
+        elif fam == 1:
+            N = max(int(round(n ** (1 / 3))), 6)
+            m = G.laplacian_3d(N, shift_seed=seed + i)
+        elif fam == 2:
+            m = G.banded_random(n, 2 + int(u[i, 5] * 15), seed=seed, problem=1000 + i)
+        else:
+            m = G.chung_lu_normalized(max(n, 1024), seed=seed + i)
+        nev = (4, 8, 16)[min(int(u[i, 3] * 3), 2)]
+        mixed = u[i, 4] < 0.7
+        reqs.append(dict(t=float(arrivals[i]), m=m, nev=nev, ncv=3 * nev, mixed=bool(mixed), fam=fam))
+    return reqs
+
+
+def run_serve(args):
+    """Continuous-batching server vs the plain FP64 solver serving the same
+    stream one request at a time (FIFO); latency = completion - arrival."""
+    import torch
+
+    import hlanc_gb300 as H
+    from hlanc_gb300 import build
+    build.build()
+    reqs = serve_requests(args.serve_count)
+    for r in reqs:
+        prec = H.HLANC_PREC_FP32_REFINE if r["mixed"] else H.HLANC_PREC_FP64
+        r["op"] = H.dcsrmv_operator_gpu(r["m"], precision=prec)
+    # warm-up: a few solves to load kernels
+    for r in reqs[:3]:
+        H.solve(r["op"], r["nev"], r["ncv"], tol=1e-10)
+
+    def stats(lat, t_total, ok_pairs):
+        lat = np.sort(np.array(lat))
+        return {"requests": len(lat), "seconds": t_total, "eigenpairs_per_s": ok_pairs / t_total,
+                "p50_s": float(np.percentile(lat, 50)), "p95_s": float(np.percentile(lat, 95)),
+                "p99_s": float(np.percentile(lat, 99))}
+
+    # server
+    srv = H.Server(mem_budget_bytes=150 << 30, max_slots=args.serve_slots)
+    t0 = time.perf_counter()
+    nxt, ids, done, lat, pairs = 0, {}, set(), [], 0
+    while len(done) < len(reqs):
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt]["t"] <= now:
+            r = reqs[nxt]
+            kw = dict(tol=1e-10, precision=H.HLANC_PREC_FP32_REFINE if r["mixed"] else H.HLANC_PREC_FP64)
+            ids[srv.submit(r["op"], r["nev"], r["ncv"], **kw)] = nxt
+            nxt += 1
+        active, waiting = srv.step()
+        for rid, i in list(ids.items()):
+            if i in done:
+                continue
+            res = srv.poll(rid)
+            if res is not None:
+                done.add(i)
+                lat.append(time.perf_counter() - t0 - reqs[i]["t"])
+                pairs += reqs[i]["nev"] if res[0] == 0 else 0
+        if active == 0 and waiting == 0 and nxt < len(reqs):
+            time.sleep(max(0.0, reqs[nxt]["t"] - (time.perf_counter() - t0)))
+    served = stats(lat, time.perf_counter() - t0, pairs)
+    srv.close()
+    # plain FP64, one at a time, FIFO over the same arrivals
+    t0 = time.perf_counter()
+    lat, pairs = [], 0
+    for r in reqs:
+        now = time.perf_counter() - t0
+        if r["t"] > now:
+            time.sleep(r["t"] - now)
+        rc, _, _, _ = H.solve(r["op"], r["nev"], r["ncv"], tol=1e-10)
+        lat.append(time.perf_counter() - t0 - r["t"])
+        pairs += r["nev"] if rc == 0 else 0
+    plain = stats(lat, time.perf_counter() - t0, pairs)
+    line = {"metric": "serving throughput (eigenpairs/s) and latency", "value": served["eigenpairs_per_s"],
+            "unit": "eigenpairs/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64 (70% fp32 SpMV)",
+            "data": "synthetic (seeded generators)",
+            "config": {"workload": f"serve{args.serve_count}", "arrivals": "Poisson, mean 200 req/s, seed 4",
+                       "n": "log-uniform [1000, 200000]", "nev": "{4,8,16}, ncv = 3 nev", "mix": "70% fp32+refine",
+                       "slots": args.serve_slots, "mem_budget_GB": 150},
+            "server": served, "plain_fp64_one_at_a_time": plain,
+            "throughput_ratio": served["eigenpairs_per_s"] / plain["eigenpairs_per_s"],
+            "p99_ratio_plain_over_server": plain["p99_s"] / served["p99_s"]}
+    print(json.dumps(line), flush=True)
+
+
 def config_of(args, wl, m):
     return {"workload": args.workload, "description": wl["desc"], "n": m.n, "nnz": m.nnz, "nev": wl["nev"],
             "ncv": wl["ncv"], "tol": wl["tol"] or "dlamch(E)", "which": "largest algebraic",
@@ -230,7 +390,18 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--full-spmv", type=int, default=0, help="SpMV count of a full solve (CPU extrapolation)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch", action="store_true", help="batched form (512 banded problems)")
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--serve", action="store_true", help="serving form (Poisson request stream)")
+    ap.add_argument("--serve-count", type=int, default=100)
+    ap.add_argument("--serve-slots", type=int, default=32)
     args = ap.parse_args()
+    if args.batch:
+        run_batch(args)
+        return
+    if args.serve:
+        run_serve(args)
+        return
     wl = WORKLOADS[args.workload]
     m = wl["gen"]()
     if args.impl == "reference":

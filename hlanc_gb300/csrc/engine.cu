@@ -1295,6 +1295,8 @@ struct hlanc_server_s {
         hlanc_stats_t stats;
         double t_submit = 0, t_admit = 0, t_done = 0;
         std::vector<double> start;
+        int phase = 0;           // 1: FP32-SpMV phase of a mixed-precision solve, 0: FP64
+        State first;             // counters of the FP32 phase
     };
     hlanc_server_opts_t opts;
     Engine E;
@@ -1335,8 +1337,10 @@ int hlanc_server_submit(hlanc_server_t s, hlanc_csr_t csr, int nev, int ncv, con
     else hlanc_opts_default(&r.o);
     if (r.o.start) r.start.assign(r.o.start, r.o.start + csr->nrows);
     r.o.start = nullptr;
-    r.o.precision = HLANC_PREC_FP64;
-    r.bytes = ProbRes::estimate(csr->nrows, ncv, 0);
+    const bool fp32 = r.o.precision == HLANC_PREC_FP32_REFINE && csr->val32_d;
+    r.o.precision = fp32 ? HLANC_PREC_FP32_REFINE : HLANC_PREC_FP64;
+    r.phase = fp32 ? 1 : 0;
+    r.bytes = ProbRes::estimate(csr->nrows, ncv, fp32 ? 1 : 0);
     if (r.bytes > s->opts.mem_budget_bytes) return HLANC_ERR_ALLOC;
     r.t_submit = now_s();
     memset(&r.stats, 0, sizeof r.stats);
@@ -1377,7 +1381,9 @@ int hlanc_server_step(hlanc_server_t s, int *n_active, int *n_pending) {
         }
         if (s->used + r.bytes > s->opts.mem_budget_bytes) break;
         int idx = 0;
-        if ((rc = E.add(r.csr->nrows, r.nev, r.ncv, r.csr, nullptr, nullptr, 0, r.o, &idx))) return rc;
+        hlanc_opts_t o1 = r.o;
+        if (r.phase == 1) o1.tol = std::max(r.o.tol > 0 ? r.o.tol : 0.0, 1e-6);   // FP32 phase tolerance
+        if ((rc = E.add(r.csr->nrows, r.nev, r.ncv, r.csr, nullptr, nullptr, r.phase, o1, &idx))) return rc;
         r.prob = idx;
         r.state = 1;
         r.t_admit = now_s();
@@ -1432,6 +1438,41 @@ int hlanc_server_step(hlanc_server_t s, int *n_active, int *n_pending) {
         if (p.hs.status != ST_RUNNING && p.hs.status == ST_CONVERGED) conv.push_back(r.prob);
     }
     if (!conv.empty() && (rc = E.finalize_many(conv))) return rc;
+    // a finished FP32 phase becomes an FP64 solve started from the sum of its
+    // Ritz vectors (or from a fresh start vector if it did not converge)
+    bool need_norm = false;
+    for (long long id : s->active) {
+        auto &r = s->reqs[id];
+        ProbRes &p = E.probs[r.prob];
+        if (r.phase != 1 || p.hs.status == ST_RUNNING) continue;
+        r.first = p.hs;
+        const bool warm = p.hs.status == ST_CONVERGED;
+        if (warm) {
+            k_sum_columns<<<304, 256, 0, E.stream>>>(p.vout, p.ldo, p.n, p.hs.nconv, p.r0);
+            launch_counter() += 1;
+        }
+        State S0 = initial_state(r.nev, r.ncv, r.o);
+        p.hs = S0;
+        p.cycles = 0;
+        p.fp32 = 0;
+        CK(cudaMemcpyAsync(p.st, &S0, sizeof S0, cudaMemcpyHostToDevice, E.stream));
+        r.phase = 0;
+        need_norm = true;
+        if (!warm) {
+            E.active.clear();
+            for (long long q : s->active) E.active.push_back(s->reqs[q].prob);
+            if ((rc = E.upload())) return rc;
+            hlanc_opts_t o = r.o;
+            if (!r.start.empty()) o.start = r.start.data();
+            if ((rc = E.start_vector(r.prob, o))) return rc;
+        }
+    }
+    if (need_norm) {
+        E.active.clear();
+        for (long long q : s->active) E.active.push_back(s->reqs[q].prob);
+        if ((rc = E.upload())) return rc;
+        if ((rc = E.norm_init())) return rc;
+    }
     for (auto it = s->active.begin(); it != s->active.end();) {
         auto &r = s->reqs[*it];
         ProbRes &p = E.probs[r.prob];
@@ -1445,7 +1486,14 @@ int hlanc_server_step(hlanc_server_t s, int *n_active, int *n_pending) {
                                  sizeof(double) * n, m, cudaMemcpyDeviceToHost, E.stream));
             CK(cudaStreamSynchronize(E.stream));
         }
-        fill_stats(&r.stats, p.hs, p, (double)r.csr->nnz, 0, 0, 0.0, r.status);
+        State S = p.hs;
+        int refine = 0;
+        if (r.o.precision == HLANC_PREC_FP32_REFINE) {
+            refine = S.iter;
+            S.spmv += r.first.spmv; S.passes += r.first.passes; S.sumc += r.first.sumc;
+            S.sumnev += r.first.sumnev; S.napply += r.first.napply;
+        }
+        fill_stats(&r.stats, S, p, (double)r.csr->nnz, r.o.precision == HLANC_PREC_FP32_REFINE, refine, 0.0, r.status);
         r.t_done = now_s();
         r.stats.seconds = r.t_done - r.t_submit;
         r.state = 2;

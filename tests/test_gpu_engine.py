@@ -181,3 +181,31 @@ def test_cpp_dropin_end_to_end(H, tmp_path, readers_golden):
         assert rc == 0, line
         vals = np.array([float(x) for x in parts[-4:]])
         assert np.abs(vals - ref).max() <= 1e-10 * np.abs(ref).max(), line
+
+
+def test_server_mixed_precision_requests(H):
+    mats = _batch_mats(6, seed=9, n_lo=1000, n_hi=5000)
+    ops = [H.dcsrmv_operator_gpu(m, precision=H.HLANC_PREC_FP32_REFINE) for m in mats]
+    srv = H.Server(mem_budget_bytes=64 << 20, max_slots=3)
+    ids = [srv.submit(op, 4, 12, precision=H.HLANC_PREC_FP32_REFINE if i % 2 == 0 else H.HLANC_PREC_FP64)
+           for i, op in enumerate(ops)]
+    results = {}
+    for _ in range(5000):
+        srv.step()
+        for i, rid in enumerate(ids):
+            if i not in results:
+                r = srv.poll(rid)
+                if r is not None:
+                    results[i] = r
+        if len(results) == len(ids):
+            break
+    assert len(results) == len(ids)
+    for i, m in enumerate(mats):
+        status, vals, vecs, st = results[i]
+        assert status == 0
+        ref = np.sort(np.linalg.eigvalsh(G.to_scipy(m).toarray()))[-4:]
+        assert np.abs(vals[:4] - ref).max() <= 1e-10 * np.abs(ref).max()
+        R = G.to_scipy(m) @ vecs[:, :4] - vecs[:, :4] * vals[:4]
+        assert np.linalg.norm(R, axis=0).max() <= 1e-10 * _norm_a(m)
+        if i % 2 == 0:
+            assert st["refine_restarts"] >= 1
