@@ -54,8 +54,14 @@ WORKLOADS = {
                      gen=lambda: G.laplacian_3d(64, shift_seed=1), nev=20, ncv=60, tol=1e-10),
     "lap2d_100": dict(desc="2-D Laplacian 100^2 (reference tolerance dlamch('E'))",
                       gen=lambda: G.laplacian_2d(100), nev=10, ncv=30, tol=0.0),
+    "chunglu_22": dict(desc="normalised adjacency of a Chung-Lu graph, n = 2^22, exponent 2.5, mean degree 32 "
+                            "(seed 2); FP32 SpMV + FP64 refinement",
+                       gen=lambda: G.chung_lu_normalized(1 << 22, seed=2), nev=16, ncv=48, tol=1e-10, mixed=True),
+    "chunglu_22_fp64": dict(desc="normalised adjacency of a Chung-Lu graph, n = 2^22 (seed 2); plain FP64",
+                            gen=lambda: G.chung_lu_normalized(1 << 22, seed=2), nev=16, ncv=48, tol=1e-10),
 }
-FULL_SOLVE_SPMV = {"lap3d_160": 3460, "lap3d_100": None, "lap3d_64": 1312, "lap2d_100": 1375}
+FULL_SOLVE_SPMV = {"lap3d_160": 3460, "lap3d_100": None, "lap3d_64": 1312, "lap2d_100": 1375,
+                   "chunglu_22": None, "chunglu_22_fp64": None}
 
 
 def _env_int(k, d):
@@ -417,7 +423,8 @@ def main():
     build.build()
     dev = local
     nev, ncv, tol = wl["nev"], wl["ncv"], wl["tol"]
-    op = H.dcsrmv_operator_gpu(m, dev=dev)
+    prec = H.HLANC_PREC_FP32_REFINE if wl.get("mixed") else H.HLANC_PREC_FP64
+    op = H.dcsrmv_operator_gpu(m, dev=dev, precision=prec)
     stream = torch.cuda.Stream()
     vals = torch.zeros(ncv, dtype=torch.float64, device="cuda")
     vecs = torch.zeros((ncv, m.n), dtype=torch.float64, device="cuda")
@@ -425,7 +432,7 @@ def main():
 
     def solve_dev(**kw):
         return H.solve_device(op, nev, ncv, vals.data_ptr(), vecs.data_ptr(), m.n, dev=dev, tol=tol,
-                              stream=stream.cuda_stream, **kw)
+                              stream=stream.cuda_stream, precision=prec, **kw)
 
     for _ in range(args.warmup):
         st = solve_dev()
@@ -456,15 +463,33 @@ def main():
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        op2 = H.dcsrmv_operator_gpu(m, dev=dev)
+        op2 = H.dcsrmv_operator_gpu(m, dev=dev, precision=prec)
         st2: dict = {}
-        rc = H.ds_solver_gpu(m.n, nev, ncv, values_h, vectors_h, m.n, op2, dev, opts_=H.opts(tol=tol), stats=st2)
+        rc = H.ds_solver_gpu(m.n, nev, ncv, values_h, vectors_h, m.n, op2, dev, opts_=H.opts(tol=tol, precision=prec),
+                             stats=st2)
         op2.close()
         e2e_ms.append((time.perf_counter() - t) * 1e3)
         valid = valid and rc == 0
     e2e_ms = allmax(pg, statistics.median(e2e_ms))
     h2d = 4 * (m.n + 1) + 12 * m.nnz
     d2h = 8 * nev + 8 * m.n * ncv
+
+    # the SpMV kernel alone (dcsrmv_operator_gpu::operator() on device vectors)
+    xs = torch.rand(m.n, dtype=torch.float64, device="cuda")
+    ys = torch.zeros_like(xs)
+    for _ in range(3):
+        op.spmv_async(xs.data_ptr(), ys.data_ptr(), stream.cuda_stream)
+    reps = 20
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(reps):
+        op.spmv_async(xs.data_ptr(), ys.data_ptr(), stream.cuda_stream)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    spmv_ms = f0.elapsed_time(f1) / reps
+    nnz_g = op.nnz_general()
+    spmv_bytes = 12.0 * nnz_g + 4.0 * (m.n + 1) + 16.0 * m.n
+    del xs, ys
 
     # roofline: one profiled solve
     pst = solve_dev(profile=True)
@@ -498,7 +523,12 @@ def main():
                       "cgs_passes": stats[-1]["cgs_passes"], "nconv": stats[-1]["nconv"]},
             "e2e": {"value": world * nev / (e2e_ms / 1e3) if valid else 0.0, "unit": "eigenpairs/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-            "roofline": roofline, "gpu_launches": launches, "clocks": clk.summary()}
+            "roofline": roofline, "gpu_launches": launches, "clocks": clk.summary(),
+            "spmv": {"us_per_call": spmv_ms * 1e3, "bytes_per_call": spmv_bytes,
+                     "achieved_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9,
+                     "frac_of_hbm": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / measured_peaks()[0],
+                     "note": "FP64 CSR SpMV alone, algorithmic bytes 12 nnz + 4(n+1) + 16 n, x/y not L2-flushed "
+                             "(x is 8n bytes of L2-resident gather)"}}
     if rank == 0 and world == 1 and not args.no_cpu:
         full = FULL_SOLVE_SPMV.get(args.workload) or stats[-1]["spmv_calls"]
         line["cpu_baseline"] = cpu_sample(m, wl, os.cpu_count() or 1, full)

@@ -15,6 +15,8 @@
 // registers over a whole tile before the (few) shuffle additions.
 #include <float.h>
 
+#include <type_traits>
+
 #include "internal.cuh"
 
 namespace hlanc {
@@ -67,6 +69,65 @@ __device__ __forceinline__ bool step_active(const State *S, int s) {
     return S->status == ST_RUNNING && S->phase == PH_EXTEND && s < S->np;
 }
 
+// ---- SpMV of 256 rows by one CTA -------------------------------------------------
+// Rows up to LONG_ROW entries: each warp stages its 32 rows' nonzeros through
+// shared memory in 256-entry chunks with coalesced loads, then every lane sums
+// its own row (one FMA per stored entry, no shuffles: GB300's FP64 pipe is the
+// scarce resource).  Longer rows are deferred and reduced by a whole warp.
+// `emit(r, acc)` receives each row's sum.
+constexpr int STAGE = 256;
+template <typename T, typename Emit>
+__device__ __forceinline__ void spmv_chunk(const int *__restrict__ rp, const int *__restrict__ ci,
+                                           const T *__restrict__ val, const T *__restrict__ x, int base,
+                                           int row_end, int *s_long, int &s_nlong, int *s_col, T *s_val,
+                                           Emit emit) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) s_nlong = 0;
+    __syncthreads();
+    const int r = base + threadIdx.x;
+    const int wr0 = base + warp * 32;
+    const int wr1 = min(wr0 + 32, row_end);
+    int a = 0, b = 0;
+    bool mine = false;
+    if (r < row_end) {
+        a = rp[r];
+        b = rp[r + 1];
+        if (b - a > LONG_ROW) s_long[atomicAdd(&s_nlong, 1)] = r;
+        else mine = true;
+    }
+    if (wr0 < wr1) {
+        const int g0 = rp[wr0], g1 = rp[wr1];
+        int *wc = s_col + warp * STAGE;
+        T *wv = s_val + warp * STAGE;
+        T acc = T(0);
+        for (int c0 = g0; c0 < g1; c0 += STAGE) {
+            const int cn = min(STAGE, g1 - c0);
+            __syncwarp();
+            for (int i = lane; i < cn; i += 32) {
+                wc[i] = ci[c0 + i];
+                wv[i] = val[c0 + i];
+            }
+            __syncwarp();
+            if (mine) {
+                const int lo = max(a, c0) - c0, hi = min(b, c0 + cn) - c0;
+                for (int i = lo; i < hi; ++i) acc = fma(wv[i], x[wc[i]], acc);
+            }
+        }
+        if (mine) emit(r, acc);
+    }
+    __syncthreads();
+    for (int q = warp; q < s_nlong; q += TPB / 32) {
+        const int rr = s_long[q];
+        const int la = rp[rr], lb = rp[rr + 1];
+        T acc = T(0);
+        for (int i = la + lane; i < lb; i += 32) acc = fma(val[i], x[ci[i]], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) emit(rr, acc);
+    }
+    __syncthreads();
+}
+
 // ---- SpMV of the step --------------------------------------------------------
 // Thread per row (one DFMA per stored entry, no shuffles); rows longer than
 // LONG_ROW are deferred and reduced by a whole warp.
@@ -85,53 +146,23 @@ __global__ void __launch_bounds__(TPB) k_spmv_step(const Problem *__restrict__ p
     const double *__restrict__ rin = step_in(P, j);
     double *__restrict__ w = step_out(P, j);
     double *__restrict__ vj = P.V + (size_t)j * P.ld;
-    const int *__restrict__ rp = P.row_ptr;
-    const int *__restrict__ ci = P.col;
     __shared__ int s_long[TPB];
     __shared__ int s_nlong;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ int s_col[(TPB / 32) * STAGE];
+    __shared__ typename std::conditional<F32, float, double>::type s_val[(TPB / 32) * STAGE];
     for (int base = t.row0; base < t.row1; base += TPB) {
-        if (threadIdx.x == 0) s_nlong = 0;
-        __syncthreads();
         const int r = base + threadIdx.x;
-        if (r < t.row1) {
-            if (!F32) {
-                const double x = rin[r];
-                vj[r] = scale ? x * t1 : x;
-            }
-            const int a = rp[r], b = rp[r + 1];
-            if (b - a > LONG_ROW) {
-                s_long[atomicAdd(&s_nlong, 1)] = r;
-            } else if (F32) {
-                const float *__restrict__ v32 = P.val32;
-                const float *__restrict__ x32 = P.x32;
-                float acc = 0.f;
-                for (int i = a; i < b; ++i) acc = fmaf(v32[i], x32[ci[i]], acc);
-                w[r] = (double)acc;
-            } else {
-                const double *__restrict__ val = P.val;
-                double acc = 0.0;
-                for (int i = a; i < b; ++i) acc = fma(val[i], rin[ci[i]], acc);
-                w[r] = scale ? acc * t1 : acc;
-            }
+        if (!F32 && r < t.row1) {
+            const double x = rin[r];
+            vj[r] = scale ? x * t1 : x;
         }
-        __syncthreads();
-        for (int q = warp; q < s_nlong; q += TPB / 32) {
-            const int rr = s_long[q];
-            const int a = rp[rr], b = rp[rr + 1];
-            if (F32) {
-                float acc = 0.f;
-                for (int i = a + lane; i < b; i += 32) acc = fmaf(P.val32[i], P.x32[ci[i]], acc);
-                acc = warp_sum_f(acc);
-                if (lane == 0) w[rr] = (double)acc;
-            } else {
-                double acc = 0.0;
-                for (int i = a + lane; i < b; i += 32) acc = fma(P.val[i], rin[ci[i]], acc);
-                acc = warp_sum(acc);
-                if (lane == 0) w[rr] = scale ? acc * t1 : acc;
-            }
+        if constexpr (F32) {
+            spmv_chunk<float>(P.row_ptr, P.col, P.val32, P.x32, base, t.row1, s_long, s_nlong, s_col, s_val,
+                              [=](int rr, float acc) { w[rr] = (double)acc; });
+        } else {
+            spmv_chunk<double>(P.row_ptr, P.col, P.val, rin, base, t.row1, s_long, s_nlong, s_col, s_val,
+                               [=](int rr, double acc) { w[rr] = scale ? acc * t1 : acc; });
         }
-        __syncthreads();
     }
 }
 
@@ -321,35 +352,13 @@ __global__ void __launch_bounds__(TPB) k_spmv_plain(const int *__restrict__ rp,
                                                     const int *__restrict__ ci,
                                                     const T *__restrict__ val, int nrows,
                                                     const T *__restrict__ x, T *__restrict__ y) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __shared__ int s_long[TPB];
     __shared__ int s_nlong;
-    for (int base = blockIdx.x * TPB; base < nrows; base += gridDim.x * TPB) {
-        if (threadIdx.x == 0) s_nlong = 0;
-        __syncthreads();
-        const int r = base + threadIdx.x;
-        if (r < nrows) {
-            const int a = rp[r], b = rp[r + 1];
-            if (b - a > LONG_ROW) {
-                s_long[atomicAdd(&s_nlong, 1)] = r;
-            } else {
-                T acc = T(0);
-                for (int i = a; i < b; ++i) acc = fma(val[i], x[ci[i]], acc);
-                y[r] = acc;
-            }
-        }
-        __syncthreads();
-        for (int q = warp; q < s_nlong; q += TPB / 32) {
-            const int rr = s_long[q];
-            const int a = rp[rr], b = rp[rr + 1];
-            T acc = T(0);
-            for (int i = a + lane; i < b; i += 32) acc = fma(val[i], x[ci[i]], acc);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) y[rr] = acc;
-        }
-        __syncthreads();
-    }
+    __shared__ int s_col[(TPB / 32) * STAGE];
+    __shared__ T s_val[(TPB / 32) * STAGE];
+    for (int base = blockIdx.x * TPB; base < nrows; base += gridDim.x * TPB)
+        spmv_chunk<T>(rp, ci, val, x, base, nrows, s_long, s_nlong, s_col, s_val,
+                      [=](int rr, T acc) { y[rr] = acc; });
 }
 
 // ---- residuals of k Ritz pairs (demo/verify_eigs.cu:52-98) ------------------
