@@ -58,8 +58,34 @@ struct hlanc_csr_s {
     double *xs_d = nullptr, *ys_d = nullptr;   // staging for host vectors (HLanc.hpp:541-549)
     cudaStream_t stream = nullptr;
     double norm_inf = 0.0;                      // max_r sum |a_rc|
+    std::vector<SpmvTile> stiles_h;             // entry-balanced SpMV work units (prob = 0)
+    SpmvTile *stiles_d = nullptr;
     std::mutex mu;
 };
+
+// Split rows into SpMV work units: at most SPMV_ROWS rows and SPMV_NNZ
+// entries each; a row with more than SPMV_NNZ entries is its own (wide) unit.
+static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &out) {
+    out.clear();
+    int r = 0;
+    while (r < nrows) {
+        const long long len = (long long)rp[r + 1] - rp[r];
+        if (len > SPMV_NNZ) {
+            out.push_back({0, r, r + 1, 1});
+            ++r;
+            continue;
+        }
+        const int r0 = r;
+        long long nnz = 0;
+        while (r < nrows && r - r0 < SPMV_ROWS) {
+            const long long l = (long long)rp[r + 1] - rp[r];
+            if (l > SPMV_NNZ || (nnz + l > SPMV_NNZ && r > r0)) break;
+            nnz += l;
+            ++r;
+        }
+        out.push_back({0, r0, r, 0});
+    }
+}
 
 struct hlanc_matrix_s {
     HLanc::dcsr_matrix_t m;
@@ -247,7 +273,8 @@ public:
     std::vector<int> active;             // problems in the launch tables, in slot order
     Problem *P_d = nullptr;
     Tile *T_d = nullptr;
-    int ntiles = 0, nslots_cap = 0, ntiles_cap = 0;
+    SpmvTile *S_d = nullptr;             // entry-balanced SpMV units of all active problems
+    int ntiles = 0, nslots_cap = 0, ntiles_cap = 0, nstiles = 0, nstiles_cap = 0;
     int max_ncv = 0;
     bool fp32_any = false;
     std::map<long long, cudaGraphExec_t> graphs;
@@ -268,6 +295,7 @@ public:
         for (auto &p : probs) p.release();
         if (P_d) cudaFree(P_d);
         if (T_d) cudaFree(T_d);
+        if (S_d) cudaFree(S_d);
         if (off_d) cudaFree(off_d);
         if (flag_d) cudaFree(flag_d);
         if (mbox_d) cudaFree(mbox_d);
@@ -316,6 +344,7 @@ public:
     int upload() {
         std::vector<Problem> P(active.size());
         std::vector<Tile> T;
+        std::vector<SpmvTile> ST;
         max_ncv = 0;
         fp32_any = false;
         off_h.assign(active.size(), 0);
@@ -344,6 +373,11 @@ public:
                 tl.pad = 0;
                 T.push_back(tl);
             }
+            if (p.csr)
+                for (SpmvTile st : p.csr->stiles_h) {
+                    st.prob = (int)a;
+                    ST.push_back(st);
+                }
             max_ncv = std::max(max_ncv, p.ncv);
             fp32_any = fp32_any || p.fp32;
             off_h[a] = off;
@@ -374,6 +408,13 @@ public:
             CK(cudaMalloc(&mbox_d, sizeof(double) * mbox_cap));
             CK(cudaMallocHost(&mbox_h, sizeof(double) * mbox_cap));
         }
+        if ((int)ST.size() > nstiles_cap || !S_d) {
+            if (S_d) cudaFree(S_d);
+            nstiles_cap = std::max<int>((int)ST.size(), 1) + 64;
+            CK(cudaMalloc(&S_d, sizeof(SpmvTile) * nstiles_cap));
+        }
+        nstiles = (int)ST.size();
+        if (!ST.empty()) CK(cudaMemcpyAsync(S_d, ST.data(), sizeof(SpmvTile) * ST.size(), cudaMemcpyHostToDevice, stream));
         ntiles = (int)T.size();
         if (!P.empty()) CK(cudaMemcpyAsync(P_d, P.data(), sizeof(Problem) * P.size(), cudaMemcpyHostToDevice, stream));
         if (!T.empty()) CK(cudaMemcpyAsync(T_d, T.data(), sizeof(Tile) * T.size(), cudaMemcpyHostToDevice, stream));
@@ -420,7 +461,7 @@ public:
         const int na = (int)active.size();
         if (!device_restart) launch_scatter(P_d, na, off_d, flag_d, mbox_d, stream);
         if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), stream);
-        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, s, fp32_any, false, stream);
+        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, stream);
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
     }
@@ -505,7 +546,7 @@ public:
             if (p.host_op(p.host_ctx, xs_h, ys_h) != 0) return HLANC_ERR_CALLBACK;
             double *w = ((j + 1) & 1) ? p.r1 : p.r0;
             CK(cudaMemcpyAsync(w, ys_h, sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
-            launch_step(P_d, T_d, ntiles, s, false, true, stream);
+            launch_step(P_d, T_d, ntiles, S_d, nstiles, s, false, true, stream);
         }
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
@@ -954,6 +995,7 @@ int hlanc_csr_create(int dev, int nrows, int ncols, int nnz, const int *row_ptr,
         ninf = std::max(ninf, s);
     }
     h->norm_inf = ninf;
+    build_spmv_tiles(grp, nrows, h->stiles_h);
     DevGuard g(dev);
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t nz = (size_t)std::max<long long>(gnnz, 1);
@@ -962,6 +1004,10 @@ int hlanc_csr_create(int dev, int nrows, int ncols, int nnz, const int *row_ptr,
     CK(cudaMalloc(&h->val_d, sizeof(double) * nz + 16));
     CK(cudaMalloc(&h->xs_d, sizeof(double) * (size_t)std::max(ncols, 1)));
     CK(cudaMalloc(&h->ys_d, sizeof(double) * (size_t)std::max(nrows, 1)));
+    CK(cudaMalloc(&h->stiles_d, sizeof(SpmvTile) * std::max<size_t>(h->stiles_h.size(), 1)));
+    if (!h->stiles_h.empty())
+        CK(cudaMemcpyAsync(h->stiles_d, h->stiles_h.data(), sizeof(SpmvTile) * h->stiles_h.size(),
+                           cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->rp_d, grp, sizeof(int) * ((size_t)nrows + 1), cudaMemcpyHostToDevice, h->stream));
     if (gnnz) {
         CK(cudaMemcpyAsync(h->ci_d, gci, sizeof(int) * gnnz, cudaMemcpyHostToDevice, h->stream));
@@ -986,6 +1032,7 @@ int hlanc_csr_destroy(hlanc_csr_t h) {
         cudaFree(h->rp_d); cudaFree(h->ci_d); cudaFree(h->val_d);
         if (h->val32_d) cudaFree(h->val32_d);
         cudaFree(h->xs_d); cudaFree(h->ys_d);
+        if (h->stiles_d) cudaFree(h->stiles_d);
         if (h->stream) cudaStreamDestroy(h->stream);
     }
     delete h;
@@ -1033,7 +1080,7 @@ int hlanc_csr_apply(hlanc_csr_t h, const double *x, double *y) {
         xx = h->xs_d;
     }
     if (!is_device_ptr(y, h->dev)) yy = h->ys_d;
-    launch_spmv(h->rp_d, h->ci_d, h->val_d, h->nrows, xx, yy, h->stream);
+    launch_spmv(h->rp_d, h->ci_d, h->val_d, h->stiles_d, (int)h->stiles_h.size(), xx, yy, h->stream);
     CK(cudaGetLastError());
     if (yy != y) CK(cudaMemcpyAsync(y, yy, sizeof(double) * h->nrows, cudaMemcpyDefault, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -1043,7 +1090,7 @@ int hlanc_csr_apply(hlanc_csr_t h, const double *x, double *y) {
 int hlanc_csr_spmv_async(hlanc_csr_t h, const double *x_d, double *y_d, void *stream) {
     if (!h || !x_d || !y_d) return HLANC_ERR_INVALID;
     DevGuard g(h->dev);
-    launch_spmv(h->rp_d, h->ci_d, h->val_d, h->nrows, x_d, y_d, (cudaStream_t)stream);
+    launch_spmv(h->rp_d, h->ci_d, h->val_d, h->stiles_d, (int)h->stiles_h.size(), x_d, y_d, (cudaStream_t)stream);
     CK(cudaGetLastError());
     return HLANC_OK;
 }
@@ -1052,7 +1099,8 @@ int hlanc_csr_spmv_f32_async(hlanc_csr_t h, const float *x_d, float *y_d, void *
     if (!h || !x_d || !y_d) return HLANC_ERR_INVALID;
     if (!h->val32_d) return HLANC_ERR_INVALID;
     DevGuard g(h->dev);
-    launch_spmv_f32(h->rp_d, h->ci_d, h->val32_d, h->nrows, x_d, y_d, (cudaStream_t)stream);
+    launch_spmv_f32(h->rp_d, h->ci_d, h->val32_d, h->stiles_d, (int)h->stiles_h.size(), x_d, y_d,
+                    (cudaStream_t)stream);
     CK(cudaGetLastError());
     return HLANC_OK;
 }

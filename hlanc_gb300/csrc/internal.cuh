@@ -87,6 +87,14 @@ struct Problem {
 
 struct Tile { int prob, row0, row1, pad; };
 
+// SpMV work unit: up to SPMV_ROWS consecutive rows holding at most
+// SPMV_NNZ stored entries, or one row longer than that (`wide`), reduced by
+// the whole CTA.  Balancing by entries keeps skewed (power-law) matrices from
+// piling their long rows onto a few CTAs.
+constexpr int SPMV_ROWS = 256;
+constexpr int SPMV_NNZ = 4096;
+struct SpmvTile { int prob, row0, row1, wide; };
+
 // ---- device helpers --------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -212,8 +220,8 @@ void prof_end(int cls, cudaStream_t s);
 void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, int prob,
                          unsigned long long seed, cudaStream_t s);
 void launch_norm_init(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s);
-void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, bool fp32_any,
-                 bool external_w, cudaStream_t s);
+void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const SpmvTile *stiles_d,
+                 int nstiles, int step, bool fp32_any, bool external_w, cudaStream_t s);
 void launch_prep_f32(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, cudaStream_t s);
 void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, double *xout,
                      cudaStream_t s);
@@ -222,10 +230,10 @@ void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_n
                   cudaStream_t s);
 void launch_finalize(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
 void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, cudaStream_t s);
-void launch_spmv(const int *row_ptr, const int *col, const double *val, int nrows, const double *x,
-                 double *y, cudaStream_t s);
-void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, int nrows,
-                     const float *x, float *y, cudaStream_t s);
+void launch_spmv(const int *row_ptr, const int *col, const double *val, const SpmvTile *stiles, int nstiles,
+                 const double *x, double *y, cudaStream_t s);
+void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, const SpmvTile *stiles,
+                     int nstiles, const float *x, float *y, cudaStream_t s);
 void launch_gather(const Problem *P_d, int nprob, const long long *off_d, double *buf_d, cudaStream_t s);
 void launch_scatter(const Problem *P_d, int nprob, const long long *off_d, const int *flag_d,
                     const double *buf_d, cudaStream_t s);

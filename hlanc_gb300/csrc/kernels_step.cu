@@ -131,10 +131,31 @@ __device__ __forceinline__ void spmv_chunk(const int *__restrict__ rp, const int
 // ---- SpMV of the step --------------------------------------------------------
 // Thread per row (one DFMA per stored entry, no shuffles); rows longer than
 // LONG_ROW are deferred and reduced by a whole warp.
+// One row longer than SPMV_NNZ entries, reduced by the whole CTA.
+template <typename T>
+__device__ __forceinline__ T spmv_wide_row(const int *__restrict__ rp, const int *__restrict__ ci,
+                                           const T *__restrict__ val, const T *__restrict__ x, int r) {
+    __shared__ T red[TPB / 32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int a = rp[r], b = rp[r + 1];
+    T acc = T(0);
+    for (int i = a + threadIdx.x; i < b; i += TPB) acc = fma(val[i], x[ci[i]], acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) red[warp] = acc;
+    __syncthreads();
+    T sum = T(0);
+    if (threadIdx.x == 0)
+        for (int w = 0; w < TPB / 32; ++w) sum += red[w];
+    return sum;   // valid in thread 0
+}
+
+// Step SpMV over the entry-balanced SpMV tiles: v_j -> V[:, j] for the
+// tile's rows, w = A v_j (FP64: A * r then one scaling per row).
 template <bool F32>
 __global__ void __launch_bounds__(TPB) k_spmv_step(const Problem *__restrict__ probs,
-                                                   const Tile *__restrict__ tiles, int s) {
-    const Tile t = tiles[blockIdx.x];
+                                                   const SpmvTile *__restrict__ tiles, int s) {
+    const SpmvTile t = tiles[blockIdx.x];
     const Problem &P = probs[t.prob];
     const State *S = P.st;
     if ((bool)P.fp32 != F32 || P.wext) return;
@@ -146,23 +167,31 @@ __global__ void __launch_bounds__(TPB) k_spmv_step(const Problem *__restrict__ p
     const double *__restrict__ rin = step_in(P, j);
     double *__restrict__ w = step_out(P, j);
     double *__restrict__ vj = P.V + (size_t)j * P.ld;
+    if (!F32)
+        for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
+            const double x = rin[r];
+            vj[r] = scale ? x * t1 : x;
+        }
+    if (t.wide) {
+        if constexpr (F32) {
+            const float acc = spmv_wide_row<float>(P.row_ptr, P.col, P.val32, P.x32, t.row0);
+            if (threadIdx.x == 0) w[t.row0] = (double)acc;
+        } else {
+            const double acc = spmv_wide_row<double>(P.row_ptr, P.col, P.val, rin, t.row0);
+            if (threadIdx.x == 0) w[t.row0] = scale ? acc * t1 : acc;
+        }
+        return;
+    }
     __shared__ int s_long[TPB];
     __shared__ int s_nlong;
     __shared__ int s_col[(TPB / 32) * STAGE];
     __shared__ typename std::conditional<F32, float, double>::type s_val[(TPB / 32) * STAGE];
-    for (int base = t.row0; base < t.row1; base += TPB) {
-        const int r = base + threadIdx.x;
-        if (!F32 && r < t.row1) {
-            const double x = rin[r];
-            vj[r] = scale ? x * t1 : x;
-        }
-        if constexpr (F32) {
-            spmv_chunk<float>(P.row_ptr, P.col, P.val32, P.x32, base, t.row1, s_long, s_nlong, s_col, s_val,
-                              [=](int rr, float acc) { w[rr] = (double)acc; });
-        } else {
-            spmv_chunk<double>(P.row_ptr, P.col, P.val, rin, base, t.row1, s_long, s_nlong, s_col, s_val,
-                               [=](int rr, double acc) { w[rr] = scale ? acc * t1 : acc; });
-        }
+    if constexpr (F32) {
+        spmv_chunk<float>(P.row_ptr, P.col, P.val32, P.x32, t.row0, t.row1, s_long, s_nlong, s_col, s_val,
+                          [=](int rr, float acc) { w[rr] = (double)acc; });
+    } else {
+        spmv_chunk<double>(P.row_ptr, P.col, P.val, rin, t.row0, t.row1, s_long, s_nlong, s_col, s_val,
+                           [=](int rr, double acc) { w[rr] = scale ? acc * t1 : acc; });
     }
 }
 
@@ -350,15 +379,21 @@ __global__ void __launch_bounds__(TPB, 6) k_apply(const Problem *__restrict__ pr
 template <typename T>
 __global__ void __launch_bounds__(TPB) k_spmv_plain(const int *__restrict__ rp,
                                                     const int *__restrict__ ci,
-                                                    const T *__restrict__ val, int nrows,
+                                                    const T *__restrict__ val,
+                                                    const SpmvTile *__restrict__ tiles,
                                                     const T *__restrict__ x, T *__restrict__ y) {
+    const SpmvTile t = tiles[blockIdx.x];
+    if (t.wide) {
+        const T acc = spmv_wide_row<T>(rp, ci, val, x, t.row0);
+        if (threadIdx.x == 0) y[t.row0] = acc;
+        return;
+    }
     __shared__ int s_long[TPB];
     __shared__ int s_nlong;
     __shared__ int s_col[(TPB / 32) * STAGE];
     __shared__ T s_val[(TPB / 32) * STAGE];
-    for (int base = blockIdx.x * TPB; base < nrows; base += gridDim.x * TPB)
-        spmv_chunk<T>(rp, ci, val, x, base, nrows, s_long, s_nlong, s_col, s_val,
-                      [=](int rr, T acc) { y[rr] = acc; });
+    spmv_chunk<T>(rp, ci, val, x, t.row0, t.row1, s_long, s_nlong, s_col, s_val,
+                  [=](int rr, T acc) { y[rr] = acc; });
 }
 
 // ---- residuals of k Ritz pairs (demo/verify_eigs.cu:52-98) ------------------
@@ -448,20 +483,20 @@ void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int st
 
 // One Lanczos step for every active problem of the tile table.  With
 // external_w the operator output was already written by the host path.
-void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, bool fp32_any,
-                 bool external_w, cudaStream_t s) {
+void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const SpmvTile *stiles_d,
+                 int nstiles, int step, bool fp32_any, bool external_w, cudaStream_t s) {
     if (!external_w) {
         if (fp32_any) {
             prof_begin(s);
             k_prep<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, 0, nullptr);
             prof_end(KC_SPMV, s);
             prof_begin(s);
-            k_spmv_step<true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step);
+            k_spmv_step<true><<<nstiles, TPB, 0, s>>>(P_d, stiles_d, step);
             prof_end(KC_SPMV, s);
             launch_counter() += 2;
         }
         prof_begin(s);
-        k_spmv_step<false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step);
+        k_spmv_step<false><<<nstiles, TPB, 0, s>>>(P_d, stiles_d, step);
         prof_end(KC_SPMV, s);
         launch_counter() += 1;
     }
@@ -476,21 +511,17 @@ void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, 
     launch_counter() += 6;
 }
 
-void launch_spmv(const int *row_ptr, const int *col, const double *val, int nrows, const double *x,
-                 double *y, cudaStream_t s) {
-    int blocks = (nrows + TPB - 1) / TPB;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    if (blocks < 1) blocks = 1;
-    k_spmv_plain<double><<<blocks, TPB, 0, s>>>(row_ptr, col, val, nrows, x, y);
+void launch_spmv(const int *row_ptr, const int *col, const double *val, const SpmvTile *stiles, int nstiles,
+                 const double *x, double *y, cudaStream_t s) {
+    if (nstiles <= 0) return;
+    k_spmv_plain<double><<<nstiles, TPB, 0, s>>>(row_ptr, col, val, stiles, x, y);
     launch_counter() += 1;
 }
 
-void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, int nrows,
-                     const float *x, float *y, cudaStream_t s) {
-    int blocks = (nrows + TPB - 1) / TPB;
-    if (blocks > 152 * 16) blocks = 152 * 16;
-    if (blocks < 1) blocks = 1;
-    k_spmv_plain<float><<<blocks, TPB, 0, s>>>(row_ptr, col, val, nrows, x, y);
+void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, const SpmvTile *stiles,
+                     int nstiles, const float *x, float *y, cudaStream_t s) {
+    if (nstiles <= 0) return;
+    k_spmv_plain<float><<<nstiles, TPB, 0, s>>>(row_ptr, col, val, stiles, x, y);
     launch_counter() += 1;
 }
 
