@@ -63,27 +63,31 @@ struct hlanc_csr_s {
     std::mutex mu;
 };
 
-// Split rows into SpMV work units: at most SPMV_ROWS rows and SPMV_NNZ
-// entries each; a row with more than SPMV_NNZ entries is its own (wide) unit.
+// Split rows into SpMV work units (see SpmvTile): runs of short rows (at most
+// SPMV_ROWS rows / SPMV_NNZ entries), runs of up to TPB/32 medium rows, and
+// single wide rows.
 static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &out) {
     out.clear();
+    auto len = [&](int r) { return (long long)rp[r + 1] - rp[r]; };
     int r = 0;
     while (r < nrows) {
-        const long long len = (long long)rp[r + 1] - rp[r];
-        if (len > SPMV_NNZ) {
-            out.push_back({0, r, r + 1, 1});
+        const long long l = len(r);
+        if (l > WIDE_ROW) {
+            out.push_back({0, r, r + 1, 2});
             ++r;
-            continue;
+        } else if (l > LONG_ROW) {
+            const int r0 = r;
+            while (r < nrows && r - r0 < TPB / 32 && len(r) > LONG_ROW && len(r) <= WIDE_ROW) ++r;
+            out.push_back({0, r0, r, 1});
+        } else {
+            const int r0 = r;
+            long long nnz = 0;
+            while (r < nrows && r - r0 < SPMV_ROWS && len(r) <= LONG_ROW && nnz + len(r) <= SPMV_NNZ) {
+                nnz += len(r);
+                ++r;
+            }
+            out.push_back({0, r0, r, 0});
         }
-        const int r0 = r;
-        long long nnz = 0;
-        while (r < nrows && r - r0 < SPMV_ROWS) {
-            const long long l = (long long)rp[r + 1] - rp[r];
-            if (l > SPMV_NNZ || (nnz + l > SPMV_NNZ && r > r0)) break;
-            nnz += l;
-            ++r;
-        }
-        out.push_back({0, r0, r, 0});
     }
 }
 

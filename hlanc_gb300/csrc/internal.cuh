@@ -87,13 +87,18 @@ struct Problem {
 
 struct Tile { int prob, row0, row1, pad; };
 
-// SpMV work unit: up to SPMV_ROWS consecutive rows holding at most
-// SPMV_NNZ stored entries, or one row longer than that (`wide`), reduced by
-// the whole CTA.  Balancing by entries keeps skewed (power-law) matrices from
-// piling their long rows onto a few CTAs.
+// SpMV work units, built once per operator from the row lengths:
+//   kind 0 (short):  up to SPMV_ROWS consecutive rows of <= LONG_ROW entries
+//                    and <= SPMV_NNZ entries in total; thread per row;
+//   kind 1 (medium): up to TPB/32 consecutive rows of LONG_ROW..WIDE_ROW
+//                    entries; warp per row;
+//   kind 2 (wide):   one row of more than WIDE_ROW entries; whole CTA.
+// Balancing by entries keeps skewed (power-law) matrices from piling their
+// long rows onto a few CTAs, and no CTA waits on a barrier for one warp.
 constexpr int SPMV_ROWS = 256;
 constexpr int SPMV_NNZ = 4096;
-struct SpmvTile { int prob, row0, row1, wide; };
+constexpr int WIDE_ROW = 2048;
+struct SpmvTile { int prob, row0, row1, kind; };
 
 // ---- device helpers --------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {

@@ -69,40 +69,32 @@ __device__ __forceinline__ bool step_active(const State *S, int s) {
     return S->status == ST_RUNNING && S->phase == PH_EXTEND && s < S->np;
 }
 
-// ---- SpMV of 256 rows by one CTA -------------------------------------------------
-// Rows up to LONG_ROW entries: each warp stages its 32 rows' nonzeros through
-// shared memory in 256-entry chunks with coalesced loads, then every lane sums
-// its own row (one FMA per stored entry, no shuffles: GB300's FP64 pipe is the
-// scarce resource).  Longer rows are deferred and reduced by a whole warp.
-// `emit(r, acc)` receives each row's sum.
+// ---- SpMV work units ----------------------------------------------------------------
+// Short rows: each warp stages its 32 rows' entries through shared memory in
+// 256-entry chunks with coalesced loads; each lane then sums its own row in
+// batches of 8 (eight independent gathers in flight, one FMA per stored entry:
+// GB300's FP64 pipe is the scarce resource, so no shuffles).
 constexpr int STAGE = 256;
 template <typename T, typename Emit>
-__device__ __forceinline__ void spmv_chunk(const int *__restrict__ rp, const int *__restrict__ ci,
-                                           const T *__restrict__ val, const T *__restrict__ x, int base,
-                                           int row_end, int *s_long, int &s_nlong, int *s_col, T *s_val,
-                                           Emit emit) {
+__device__ __forceinline__ void spmv_short(const int *__restrict__ rp, const int *__restrict__ ci,
+                                           const T *__restrict__ val, const T *__restrict__ x, int row0,
+                                           int row1, int *s_col, T *s_val, Emit emit) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) s_nlong = 0;
-    __syncthreads();
-    const int r = base + threadIdx.x;
-    const int wr0 = base + warp * 32;
-    const int wr1 = min(wr0 + 32, row_end);
-    int a = 0, b = 0;
-    bool mine = false;
-    if (r < row_end) {
-        a = rp[r];
-        b = rp[r + 1];
-        if (b - a > LONG_ROW) s_long[atomicAdd(&s_nlong, 1)] = r;
-        else mine = true;
-    }
-    if (wr0 < wr1) {
-        const int g0 = rp[wr0], g1 = rp[wr1];
-        int *wc = s_col + warp * STAGE;
-        T *wv = s_val + warp * STAGE;
+    int *wc = s_col + warp * STAGE;
+    T *wv = s_val + warp * STAGE;
+    for (int wr0 = row0 + warp * 32; wr0 < row1; wr0 += TPB) {
+        const int r = wr0 + lane;
+        const bool mine = r < row1;
+        const int a = mine ? rp[r] : 0;
+        const int b = mine ? rp[r + 1] : 0;
+        const int nvalid = min(32, row1 - wr0);
+        const int g0 = __shfl_sync(0xffffffffu, a, 0);
+        const int g1 = __shfl_sync(0xffffffffu, b, nvalid - 1);
         T acc = T(0);
         for (int c0 = g0; c0 < g1; c0 += STAGE) {
             const int cn = min(STAGE, g1 - c0);
             __syncwarp();
+#pragma unroll 4
             for (int i = lane; i < cn; i += 32) {
                 wc[i] = ci[c0 + i];
                 wv[i] = val[c0 + i];
@@ -110,88 +102,125 @@ __device__ __forceinline__ void spmv_chunk(const int *__restrict__ rp, const int
             __syncwarp();
             if (mine) {
                 const int lo = max(a, c0) - c0, hi = min(b, c0 + cn) - c0;
-                for (int i = lo; i < hi; ++i) acc = fma(wv[i], x[wc[i]], acc);
+                for (int i = lo; i < hi; i += 8) {
+                    T xv[8], vv[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const bool ok = i + q < hi;
+                        vv[q] = ok ? wv[i + q] : T(0);
+                        xv[q] = ok ? x[wc[i + q]] : T(0);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (i + q < hi) acc = fma(vv[q], xv[q], acc);
+                }
             }
         }
         if (mine) emit(r, acc);
     }
-    __syncthreads();
-    for (int q = warp; q < s_nlong; q += TPB / 32) {
-        const int rr = s_long[q];
-        const int la = rp[rr], lb = rp[rr + 1];
-        T acc = T(0);
-        for (int i = la + lane; i < lb; i += 32) acc = fma(val[i], x[ci[i]], acc);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) emit(rr, acc);
-    }
-    __syncthreads();
 }
 
-// ---- SpMV of the step --------------------------------------------------------
-// Thread per row (one DFMA per stored entry, no shuffles); rows longer than
-// LONG_ROW are deferred and reduced by a whole warp.
-// One row longer than SPMV_NNZ entries, reduced by the whole CTA.
+// Medium rows: warp per row, no barrier.
+template <typename T, typename Emit>
+__device__ __forceinline__ void spmv_medium(const int *__restrict__ rp, const int *__restrict__ ci,
+                                            const T *__restrict__ val, const T *__restrict__ x, int row0,
+                                            int row1, Emit emit) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = row0 + warp; r < row1; r += TPB / 32) {
+        const int a = rp[r], b = rp[r + 1];
+        T acc = T(0);
+#pragma unroll 4
+        for (int i = a + lane; i < b; i += 32) acc = fma(val[i], x[ci[i]], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) emit(r, acc);
+    }
+}
+
+// Wide row: whole CTA; the sum is valid in thread 0.
 template <typename T>
-__device__ __forceinline__ T spmv_wide_row(const int *__restrict__ rp, const int *__restrict__ ci,
-                                           const T *__restrict__ val, const T *__restrict__ x, int r) {
-    __shared__ T red[TPB / 32];
+__device__ __forceinline__ T spmv_wide(const int *__restrict__ rp, const int *__restrict__ ci,
+                                       const T *__restrict__ val, const T *__restrict__ x, int r, T *red) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int a = rp[r], b = rp[r + 1];
     T acc = T(0);
+#pragma unroll 4
     for (int i = a + threadIdx.x; i < b; i += TPB) acc = fma(val[i], x[ci[i]], acc);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __syncthreads();
     if (lane == 0) red[warp] = acc;
     __syncthreads();
     T sum = T(0);
     if (threadIdx.x == 0)
         for (int w = 0; w < TPB / 32; ++w) sum += red[w];
-    return sum;   // valid in thread 0
+    return sum;
 }
 
-// Step SpMV over the entry-balanced SpMV tiles: v_j -> V[:, j] for the
-// tile's rows, w = A v_j (FP64: A * r then one scaling per row).
+template <typename T, typename Emit>
+__device__ __forceinline__ void spmv_unit(const SpmvTile &t, const int *__restrict__ rp, const int *__restrict__ ci,
+                                          const T *__restrict__ val, const T *__restrict__ x, int *s_col,
+                                          T *s_val, T *red, Emit emit) {
+    if (t.kind == 0) {
+        spmv_short<T>(rp, ci, val, x, t.row0, t.row1, s_col, s_val, emit);
+    } else if (t.kind == 1) {
+        spmv_medium<T>(rp, ci, val, x, t.row0, t.row1, emit);
+    } else {
+        const T acc = spmv_wide<T>(rp, ci, val, x, t.row0, red);
+        if (threadIdx.x == 0) emit(t.row0, acc);
+    }
+}
+
+// ---- SpMV of the step --------------------------------------------------------
+// Persistent over the SpMV units of all problems; a CTA re-reads a problem's
+// state only when its next unit belongs to another problem.
+// v_j -> V[:, j] for the unit's rows, w = A v_j (FP64: A r, one scaling per row).
 template <bool F32>
 __global__ void __launch_bounds__(TPB) k_spmv_step(const Problem *__restrict__ probs,
-                                                   const SpmvTile *__restrict__ tiles, int s) {
-    const SpmvTile t = tiles[blockIdx.x];
-    const Problem &P = probs[t.prob];
-    const State *S = P.st;
-    if ((bool)P.fp32 != F32 || P.wext) return;
-    if (!step_active(S, s)) return;
-    const int j = S->k + s;
-    const double rn = S->rnorm;
-    const bool scale = rn > DBL_MIN;
-    const double t1 = scale ? 1.0 / rn : 1.0;
-    const double *__restrict__ rin = step_in(P, j);
-    double *__restrict__ w = step_out(P, j);
-    double *__restrict__ vj = P.V + (size_t)j * P.ld;
-    if (!F32)
-        for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
-            const double x = rin[r];
-            vj[r] = scale ? x * t1 : x;
-        }
-    if (t.wide) {
-        if constexpr (F32) {
-            const float acc = spmv_wide_row<float>(P.row_ptr, P.col, P.val32, P.x32, t.row0);
-            if (threadIdx.x == 0) w[t.row0] = (double)acc;
-        } else {
-            const double acc = spmv_wide_row<double>(P.row_ptr, P.col, P.val, rin, t.row0);
-            if (threadIdx.x == 0) w[t.row0] = scale ? acc * t1 : acc;
-        }
-        return;
-    }
-    __shared__ int s_long[TPB];
-    __shared__ int s_nlong;
+                                                   const SpmvTile *__restrict__ tiles, int ntiles, int s) {
+    using T = typename std::conditional<F32, float, double>::type;
     __shared__ int s_col[(TPB / 32) * STAGE];
-    __shared__ typename std::conditional<F32, float, double>::type s_val[(TPB / 32) * STAGE];
-    if constexpr (F32) {
-        spmv_chunk<float>(P.row_ptr, P.col, P.val32, P.x32, t.row0, t.row1, s_long, s_nlong, s_col, s_val,
-                          [=](int rr, float acc) { w[rr] = (double)acc; });
-    } else {
-        spmv_chunk<double>(P.row_ptr, P.col, P.val, rin, t.row0, t.row1, s_long, s_nlong, s_col, s_val,
-                           [=](int rr, double acc) { w[rr] = scale ? acc * t1 : acc; });
+    __shared__ T s_val[(TPB / 32) * STAGE];
+    __shared__ T red[TPB / 32];
+    int cur = -1;
+    bool active = false, scale = false;
+    double t1 = 1.0;
+    const double *rin = nullptr;
+    double *w = nullptr, *vj = nullptr;
+    const Problem *P = nullptr;
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+        const SpmvTile t = tiles[ti];
+        if (t.prob != cur) {
+            cur = t.prob;
+            P = probs + cur;
+            const State *S = P->st;
+            active = (bool)P->fp32 == F32 && !P->wext && step_active(S, s);
+            if (active) {
+                const int j = S->k + s;
+                const double rn = S->rnorm;
+                scale = rn > DBL_MIN;
+                t1 = scale ? 1.0 / rn : 1.0;
+                rin = step_in(*P, j);
+                w = step_out(*P, j);
+                vj = P->V + (size_t)j * P->ld;
+            }
+        }
+        if (!active) continue;
+        if (!F32)
+            for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
+                const double x = rin[r];
+                vj[r] = scale ? x * t1 : x;
+            }
+        if constexpr (F32) {
+            spmv_unit<float>(t, P->row_ptr, P->col, P->val32, P->x32, s_col, s_val, red,
+                             [=](int rr, float acc) { w[rr] = (double)acc; });
+        } else {
+            const bool sc = scale;
+            const double tt = t1;
+            double *ww = w;
+            spmv_unit<double>(t, P->row_ptr, P->col, P->val, rin, s_col, s_val, red,
+                              [=](int rr, double acc) { ww[rr] = sc ? acc * tt : acc; });
+        }
     }
 }
 
@@ -380,20 +409,13 @@ template <typename T>
 __global__ void __launch_bounds__(TPB) k_spmv_plain(const int *__restrict__ rp,
                                                     const int *__restrict__ ci,
                                                     const T *__restrict__ val,
-                                                    const SpmvTile *__restrict__ tiles,
+                                                    const SpmvTile *__restrict__ tiles, int ntiles,
                                                     const T *__restrict__ x, T *__restrict__ y) {
-    const SpmvTile t = tiles[blockIdx.x];
-    if (t.wide) {
-        const T acc = spmv_wide_row<T>(rp, ci, val, x, t.row0);
-        if (threadIdx.x == 0) y[t.row0] = acc;
-        return;
-    }
-    __shared__ int s_long[TPB];
-    __shared__ int s_nlong;
     __shared__ int s_col[(TPB / 32) * STAGE];
     __shared__ T s_val[(TPB / 32) * STAGE];
-    spmv_chunk<T>(rp, ci, val, x, t.row0, t.row1, s_long, s_nlong, s_col, s_val,
-                  [=](int rr, T acc) { y[rr] = acc; });
+    __shared__ T red[TPB / 32];
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
+        spmv_unit<T>(tiles[ti], rp, ci, val, x, s_col, s_val, red, [=](int rr, T acc) { y[rr] = acc; });
 }
 
 // ---- residuals of k Ritz pairs (demo/verify_eigs.cu:52-98) ------------------
@@ -450,6 +472,9 @@ __global__ void k_residuals_final(const double *__restrict__ part, int nblk, int
 }
 
 // ---- launchers --------------------------------------------------------------
+// persistent SpMV grid: 6 CTAs per SM (152 SMs) or fewer when there is less work
+static int spmv_grid(int nstiles) { return nstiles < 152 * 6 ? (nstiles > 0 ? nstiles : 1) : 152 * 6; }
+
 void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, int prob,
                          unsigned long long seed, cudaStream_t s) {
     const unsigned long long key = sm_mix(seed * 0xD1B54A32D192ED03ULL + 0ULL);
@@ -491,12 +516,12 @@ void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const Spmv
             k_prep<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, 0, nullptr);
             prof_end(KC_SPMV, s);
             prof_begin(s);
-            k_spmv_step<true><<<nstiles, TPB, 0, s>>>(P_d, stiles_d, step);
+            k_spmv_step<true><<<spmv_grid(nstiles), TPB, 0, s>>>(P_d, stiles_d, nstiles, step);
             prof_end(KC_SPMV, s);
             launch_counter() += 2;
         }
         prof_begin(s);
-        k_spmv_step<false><<<nstiles, TPB, 0, s>>>(P_d, stiles_d, step);
+        k_spmv_step<false><<<spmv_grid(nstiles), TPB, 0, s>>>(P_d, stiles_d, nstiles, step);
         prof_end(KC_SPMV, s);
         launch_counter() += 1;
     }
@@ -514,14 +539,14 @@ void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const Spmv
 void launch_spmv(const int *row_ptr, const int *col, const double *val, const SpmvTile *stiles, int nstiles,
                  const double *x, double *y, cudaStream_t s) {
     if (nstiles <= 0) return;
-    k_spmv_plain<double><<<nstiles, TPB, 0, s>>>(row_ptr, col, val, stiles, x, y);
+    k_spmv_plain<double><<<spmv_grid(nstiles), TPB, 0, s>>>(row_ptr, col, val, stiles, nstiles, x, y);
     launch_counter() += 1;
 }
 
 void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, const SpmvTile *stiles,
                      int nstiles, const float *x, float *y, cudaStream_t s) {
     if (nstiles <= 0) return;
-    k_spmv_plain<float><<<nstiles, TPB, 0, s>>>(row_ptr, col, val, stiles, x, y);
+    k_spmv_plain<float><<<spmv_grid(nstiles), TPB, 0, s>>>(row_ptr, col, val, stiles, nstiles, x, y);
     launch_counter() += 1;
 }
 
