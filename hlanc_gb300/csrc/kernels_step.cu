@@ -70,53 +70,32 @@ __device__ __forceinline__ bool step_active(const State *S, int s) {
 }
 
 // ---- SpMV work units ----------------------------------------------------------------
-// Short rows: each warp stages its 32 rows' entries through shared memory in
-// 256-entry chunks with coalesced loads; each lane then sums its own row in
-// batches of 8 (eight independent gathers in flight, one FMA per stored entry:
-// GB300's FP64 pipe is the scarce resource, so no shuffles).
+// Short rows: thread per row, entries read directly in batches of 8 so eight
+// independent gathers of x are in flight per thread; one FMA per stored entry
+// and no shuffles (GB300's FP64 pipe is the scarce resource).  Measured in the
+// solver on GB300 this beats staging the rows through shared memory (the
+// staged form waits on its copies before the gathers can start).
 constexpr int STAGE = 256;
 template <typename T, typename Emit>
 __device__ __forceinline__ void spmv_short(const int *__restrict__ rp, const int *__restrict__ ci,
                                            const T *__restrict__ val, const T *__restrict__ x, int row0,
-                                           int row1, int *s_col, T *s_val, Emit emit) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int *wc = s_col + warp * STAGE;
-    T *wv = s_val + warp * STAGE;
-    for (int wr0 = row0 + warp * 32; wr0 < row1; wr0 += TPB) {
-        const int r = wr0 + lane;
-        const bool mine = r < row1;
-        const int a = mine ? rp[r] : 0;
-        const int b = mine ? rp[r + 1] : 0;
-        const int nvalid = min(32, row1 - wr0);
-        const int g0 = __shfl_sync(0xffffffffu, a, 0);
-        const int g1 = __shfl_sync(0xffffffffu, b, nvalid - 1);
+                                           int row1, int *, T *, Emit emit) {
+    for (int r = row0 + threadIdx.x; r < row1; r += TPB) {
+        const int a = rp[r], b = rp[r + 1];
         T acc = T(0);
-        for (int c0 = g0; c0 < g1; c0 += STAGE) {
-            const int cn = min(STAGE, g1 - c0);
-            __syncwarp();
-#pragma unroll 4
-            for (int i = lane; i < cn; i += 32) {
-                wc[i] = ci[c0 + i];
-                wv[i] = val[c0 + i];
-            }
-            __syncwarp();
-            if (mine) {
-                const int lo = max(a, c0) - c0, hi = min(b, c0 + cn) - c0;
-                for (int i = lo; i < hi; i += 8) {
-                    T xv[8], vv[8];
+        for (int i = a; i < b; i += 8) {
+            T xv[8], vv[8];
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const bool ok = i + q < hi;
-                        vv[q] = ok ? wv[i + q] : T(0);
-                        xv[q] = ok ? x[wc[i + q]] : T(0);
-                    }
-#pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        if (i + q < hi) acc = fma(vv[q], xv[q], acc);
-                }
+            for (int q = 0; q < 8; ++q) {
+                const bool ok = i + q < b;
+                vv[q] = ok ? val[i + q] : T(0);
+                xv[q] = ok ? x[ci[i + q]] : T(0);
             }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (i + q < b) acc = fma(vv[q], xv[q], acc);
         }
-        if (mine) emit(r, acc);
+        emit(r, acc);
     }
 }
 
@@ -172,55 +151,37 @@ __device__ __forceinline__ void spmv_unit(const SpmvTile &t, const int *__restri
 }
 
 // ---- SpMV of the step --------------------------------------------------------
-// Persistent over the SpMV units of all problems; a CTA re-reads a problem's
-// state only when its next unit belongs to another problem.
+// One CTA per SpMV unit (the hardware scheduler balances skewed units).
 // v_j -> V[:, j] for the unit's rows, w = A v_j (FP64: A r, one scaling per row).
 template <bool F32>
-__global__ void __launch_bounds__(TPB) k_spmv_step(const Problem *__restrict__ probs,
+__global__ void __launch_bounds__(TPB, 1) k_spmv_step(const Problem *__restrict__ probs,
                                                    const SpmvTile *__restrict__ tiles, int ntiles, int s) {
     using T = typename std::conditional<F32, float, double>::type;
     __shared__ int s_col[(TPB / 32) * STAGE];
     __shared__ T s_val[(TPB / 32) * STAGE];
     __shared__ T red[TPB / 32];
-    int cur = -1;
-    bool active = false, scale = false;
-    double t1 = 1.0;
-    const double *rin = nullptr;
-    double *w = nullptr, *vj = nullptr;
-    const Problem *P = nullptr;
-    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
-        const SpmvTile t = tiles[ti];
-        if (t.prob != cur) {
-            cur = t.prob;
-            P = probs + cur;
-            const State *S = P->st;
-            active = (bool)P->fp32 == F32 && !P->wext && step_active(S, s);
-            if (active) {
-                const int j = S->k + s;
-                const double rn = S->rnorm;
-                scale = rn > DBL_MIN;
-                t1 = scale ? 1.0 / rn : 1.0;
-                rin = step_in(*P, j);
-                w = step_out(*P, j);
-                vj = P->V + (size_t)j * P->ld;
-            }
+    const SpmvTile t = tiles[blockIdx.x];
+    const Problem &P = probs[t.prob];
+    const State *S = P.st;
+    if ((bool)P.fp32 != F32 || P.wext || !step_active(S, s)) return;
+    const int j = S->k + s;
+    const double rn = S->rnorm;
+    const bool scale = rn > DBL_MIN;
+    const double t1 = scale ? 1.0 / rn : 1.0;
+    const double *__restrict__ rin = step_in(P, j);
+    double *__restrict__ w = step_out(P, j);
+    double *__restrict__ vj = P.V + (size_t)j * P.ld;
+    if (!F32)
+        for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
+            const double x = rin[r];
+            vj[r] = scale ? x * t1 : x;
         }
-        if (!active) continue;
-        if (!F32)
-            for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
-                const double x = rin[r];
-                vj[r] = scale ? x * t1 : x;
-            }
-        if constexpr (F32) {
-            spmv_unit<float>(t, P->row_ptr, P->col, P->val32, P->x32, s_col, s_val, red,
-                             [=](int rr, float acc) { w[rr] = (double)acc; });
-        } else {
-            const bool sc = scale;
-            const double tt = t1;
-            double *ww = w;
-            spmv_unit<double>(t, P->row_ptr, P->col, P->val, rin, s_col, s_val, red,
-                              [=](int rr, double acc) { ww[rr] = sc ? acc * tt : acc; });
-        }
+    if constexpr (F32) {
+        spmv_unit<float>(t, P.row_ptr, P.col, P.val32, P.x32, s_col, s_val, red,
+                         [=](int rr, float acc) { w[rr] = (double)acc; });
+    } else {
+        spmv_unit<double>(t, P.row_ptr, P.col, P.val, rin, s_col, s_val, red,
+                          [=](int rr, double acc) { w[rr] = scale ? acc * t1 : acc; });
     }
 }
 
@@ -406,7 +367,7 @@ __global__ void __launch_bounds__(TPB, 6) k_apply(const Problem *__restrict__ pr
 
 // ---- standalone SpMV (operator() of dcsrmv_operator_gpu) -------------------
 template <typename T>
-__global__ void __launch_bounds__(TPB) k_spmv_plain(const int *__restrict__ rp,
+__global__ void __launch_bounds__(TPB, 1) k_spmv_plain(const int *__restrict__ rp,
                                                     const int *__restrict__ ci,
                                                     const T *__restrict__ val,
                                                     const SpmvTile *__restrict__ tiles, int ntiles,
@@ -472,8 +433,7 @@ __global__ void k_residuals_final(const double *__restrict__ part, int nblk, int
 }
 
 // ---- launchers --------------------------------------------------------------
-// persistent SpMV grid: 6 CTAs per SM (152 SMs) or fewer when there is less work
-static int spmv_grid(int nstiles) { return nstiles < 152 * 6 ? (nstiles > 0 ? nstiles : 1) : 152 * 6; }
+static int spmv_grid(int nstiles) { return nstiles > 0 ? nstiles : 1; }
 
 void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, int prob,
                          unsigned long long seed, cudaStream_t s) {
