@@ -380,6 +380,10 @@ static double dnrm2(long n, const double *x) {
     return sqrt(s);
 }
 
+/* Row blocks that keep a slice of x (or y) in a core's L1 while every
+ * column streams past it once. */
+#define ORACLE_ROW_BLOCK 2048
+
 /* y[0:c) = V[:, 0:c)^T x   (cblas_dgemv Trans, alpha=1, beta=0) */
 static void gemv_t(long n, int c, const double *v, long ldv, const double *x, double *y) {
     for (int k = 0; k < c; ++k) y[k] = 0.0;
@@ -388,15 +392,6 @@ static void gemv_t(long n, int c, const double *v, long ldv, const double *x, do
 #else
     int nt = 1;
 #endif
-    if (nt <= 1) {
-        for (int k = 0; k < c; ++k) {
-            const double *vk = v + (long)k * ldv;
-            double s = 0.0;
-            for (long i = 0; i < n; ++i) s += vk[i] * x[i];
-            y[k] = s;
-        }
-        return;
-    }
     double *part = (double *)calloc((size_t)nt * (size_t)c, sizeof(double));
 #pragma omp parallel num_threads(nt)
     {
@@ -407,11 +402,15 @@ static void gemv_t(long n, int c, const double *v, long ldv, const double *x, do
         int t = 0, T = 1;
 #endif
         long lo = n * t / T, hi = n * (t + 1) / T;
-        for (int k = 0; k < c; ++k) {
-            const double *vk = v + (long)k * ldv;
-            double s = 0.0;
-            for (long i = lo; i < hi; ++i) s += vk[i] * x[i];
-            part[(size_t)t * c + k] = s;
+        double *pk = part + (size_t)t * c;
+        for (long b = lo; b < hi; b += ORACLE_ROW_BLOCK) {
+            long e = b + ORACLE_ROW_BLOCK < hi ? b + ORACLE_ROW_BLOCK : hi;
+            for (int k = 0; k < c; ++k) {
+                const double *vk = v + (long)k * ldv;
+                double s = 0.0;
+                for (long i = b; i < e; ++i) s += vk[i] * x[i];
+                pk[k] += s;
+            }
         }
     }
     for (int t = 0; t < nt; ++t)
@@ -419,14 +418,21 @@ static void gemv_t(long n, int c, const double *v, long ldv, const double *x, do
     free(part);
 }
 
-/* y = beta*y + alpha * V[:, 0:c) x   (cblas_dgemv NoTrans) */
+/* y = beta*y + alpha * V[:, 0:c) x   (cblas_dgemv NoTrans), column-axpy
+ * form over row blocks */
 static void gemv_n(long n, int c, double alpha, const double *v, long ldv, const double *x,
                    double beta, double *y) {
 #pragma omp parallel for schedule(static) if (n > 65536)
-    for (long i = 0; i < n; ++i) {
-        double s = 0.0;
-        for (int k = 0; k < c; ++k) s += v[i + (long)k * ldv] * x[k];
-        y[i] = (beta == 0.0 ? 0.0 : beta * y[i]) + alpha * s;
+    for (long b = 0; b < n; b += ORACLE_ROW_BLOCK) {
+        long e = b + ORACLE_ROW_BLOCK < n ? b + ORACLE_ROW_BLOCK : n;
+        double acc[ORACLE_ROW_BLOCK];
+        for (long i = b; i < e; ++i) acc[i - b] = 0.0;
+        for (int k = 0; k < c; ++k) {
+            const double *vk = v + (long)k * ldv;
+            const double xk = x[k];
+            for (long i = b; i < e; ++i) acc[i - b] += vk[i] * xk;
+        }
+        for (long i = b; i < e; ++i) y[i] = (beta == 0.0 ? 0.0 : beta * y[i]) + alpha * acc[i - b];
     }
 }
 
