@@ -210,50 +210,55 @@ __global__ void __launch_bounds__(TPB) k_prep(const Problem *__restrict__ probs,
 }
 
 // ---- CGS projection: h = V[:, 0:c)^T w  (+ ||w||^2 on pass 1) ----------------
-// Warp w owns columns k = w + 8 i (i < CPW = ceil(c / 8)); lane l owns rows
-// l and l+32 of every 64-row chunk, so every V load is a coalesced 256-byte
-// warp access.  The column count per warp is a template parameter picked on
-// the device from c: no FP64 instruction is issued for a column that does
-// not exist (predicated-off FP64 instructions still occupy GB300's FP64
-// pipe).  Accumulators stay in registers for the whole tile; one transposed
-// shuffle reduction per 8 columns ends the tile.
-template <int CPW>
-__device__ __forceinline__ void proj_tile(const Problem &P, const Tile &t, const double *__restrict__ w, int c0,
-                                          int cc, bool with_norm, double *red) {
+// Thread per row, columns in panels of at most 16: each thread keeps one
+// accumulator per panel column for all the rows it visits in the tile (one
+// FP64 FMA per loaded element, coalesced column reads), then one transposed
+// warp reduction per 8 columns and a cross-warp sum in shared memory.  The
+// panel width is a template parameter picked from the device-known column
+// count, so no FP64 instruction is issued for an absent column
+// (predicated-off FP64 instructions still occupy GB300's FP64 pipe).  Measured
+// on GB300 against warp-per-column layouts and 8/24/32-column panels, 16
+// columns (64 registers, 4 CTAs per SM) was fastest.
+// Panel of NC (<= 16) consecutive columns starting at c0.
+template <int NC>
+__device__ __forceinline__ void proj_rows(const Problem &P, const Tile &t, const double *__restrict__ w, int c0,
+                                          bool with_norm, double *red, double *sm) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t ld = (size_t)P.ld;
-    double acc[8];
+    constexpr int NA = (NC + 7) / 8 * 8;
+    double acc[NA];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) acc[i] = 0.0;
+    for (int i = 0; i < NA; ++i) acc[i] = 0.0;
     double nrm = 0.0;
-    const bool last_full = warp + 8 * (CPW - 1) < cc;    // warp-uniform
-    for (int r = t.row0; r < t.row1; r += 64) {
-        const double w0 = w[r + lane];
-        const double w1 = w[r + 32 + lane];
-        if (with_norm && warp == 0) {
-            nrm = fma(w0, w0, nrm);
-            nrm = fma(w1, w1, nrm);
-        }
-        const double *__restrict__ vb = P.V + r + lane + (size_t)(c0 + warp) * ld;
+    for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
+        const double wr = w[r];
+        if (with_norm) nrm = fma(wr, wr, nrm);
+        const double *__restrict__ vr = P.V + r + (size_t)c0 * ld;
 #pragma unroll
-        for (int i = 0; i < CPW - 1; ++i) {
-            const double *vk = vb + (size_t)(8 * i) * ld;
-            acc[i] = fma(__ldcs(vk), w0, acc[i]);
-            acc[i] = fma(__ldcs(vk + 32), w1, acc[i]);
-        }
-        if (last_full) {
-            const double *vk = vb + (size_t)(8 * (CPW - 1)) * ld;
-            acc[CPW - 1] = fma(__ldcs(vk), w0, acc[CPW - 1]);
-            acc[CPW - 1] = fma(__ldcs(vk + 32), w1, acc[CPW - 1]);
-        }
+        for (int k = 0; k < NC; ++k) acc[k] = fma(__ldcs(vr + (size_t)k * ld), wr, acc[k]);
     }
-    const double v = warp_reduce8(acc);                  // column c0 + warp + 8 * (lane >> 2)
-    const int k = warp + 8 * (lane >> 2);
-    if ((lane & 3) == 0 && k < cc) red[c0 + k] = v;
-    if (with_norm && warp == 0) {
+    // lane l holds, per group g of 8 columns, the warp sum of column 8g + (l >> 2)
+#pragma unroll
+    for (int g = 0; g < NA / 8; ++g) {
+        const double v = warp_reduce8(acc + 8 * g);
+        if ((lane & 3) == 0) sm[warp * 32 + 8 * g + (lane >> 2)] = v;
+    }
+    if (with_norm) {
         nrm = warp_sum(nrm);
-        if (lane == 0) red[c0 + cc] = nrm;
+        if (lane == 0) sm[8 * 32 + warp] = nrm;
     }
+    __syncthreads();
+    if (threadIdx.x < NC) {
+        double s = 0.0;
+        for (int q = 0; q < TPB / 32; ++q) s += sm[q * 32 + threadIdx.x];
+        red[c0 + threadIdx.x] = s;
+    }
+    if (with_norm && threadIdx.x == 32) {
+        double s = 0.0;
+        for (int q = 0; q < TPB / 32; ++q) s += sm[8 * 32 + q];
+        red[c0 + NC] = s;
+    }
+    __syncthreads();
 }
 
 __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ probs,
@@ -268,19 +273,28 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
     const int m = P.ncv;
     const double *__restrict__ w = step_out(P, j);
     __shared__ double red[MAXNCV + 1], tot[MAXNCV + 1];
-    // panels of up to 64 columns (8 per warp); the norm rides on the last panel
-    for (int c0 = 0; c0 < c; c0 += 64) {
-        const int cc = min(64, c - c0);
+    __shared__ double sm[9 * 32];
+    for (int c0 = 0; c0 < c; c0 += 16) {
+        const int cc = min(16, c - c0);
         const bool nrm = pass == 1 && c0 + cc == c;
-        switch ((cc + 7) >> 3) {
-        case 1: proj_tile<1>(P, t, w, c0, cc, nrm, red); break;
-        case 2: proj_tile<2>(P, t, w, c0, cc, nrm, red); break;
-        case 3: proj_tile<3>(P, t, w, c0, cc, nrm, red); break;
-        case 4: proj_tile<4>(P, t, w, c0, cc, nrm, red); break;
-        case 5: proj_tile<5>(P, t, w, c0, cc, nrm, red); break;
-        case 6: proj_tile<6>(P, t, w, c0, cc, nrm, red); break;
-        case 7: proj_tile<7>(P, t, w, c0, cc, nrm, red); break;
-        default: proj_tile<8>(P, t, w, c0, cc, nrm, red); break;
+        switch (cc) {
+        case 1: proj_rows<1>(P, t, w, c0, nrm, red, sm); break;
+        case 2: proj_rows<2>(P, t, w, c0, nrm, red, sm); break;
+        case 3: proj_rows<3>(P, t, w, c0, nrm, red, sm); break;
+        case 4: proj_rows<4>(P, t, w, c0, nrm, red, sm); break;
+        case 5: proj_rows<5>(P, t, w, c0, nrm, red, sm); break;
+        case 6: proj_rows<6>(P, t, w, c0, nrm, red, sm); break;
+        case 7: proj_rows<7>(P, t, w, c0, nrm, red, sm); break;
+        case 8: proj_rows<8>(P, t, w, c0, nrm, red, sm); break;
+        case 9: proj_rows<9>(P, t, w, c0, nrm, red, sm); break;
+        case 10: proj_rows<10>(P, t, w, c0, nrm, red, sm); break;
+        case 11: proj_rows<11>(P, t, w, c0, nrm, red, sm); break;
+        case 12: proj_rows<12>(P, t, w, c0, nrm, red, sm); break;
+        case 13: proj_rows<13>(P, t, w, c0, nrm, red, sm); break;
+        case 14: proj_rows<14>(P, t, w, c0, nrm, red, sm); break;
+        case 15: proj_rows<15>(P, t, w, c0, nrm, red, sm); break;
+        case 16: proj_rows<16>(P, t, w, c0, nrm, red, sm); break;
+        default: break;
         }
     }
     __syncthreads();
