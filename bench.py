@@ -317,13 +317,13 @@ def serve_requests(count, seed=4, rate=200.0, n_lo=1000, n_hi=200000):
 
 def run_serve(args):
     """Continuous-batching server vs the plain FP64 solver serving the same
-    stream one request at a time (FIFO); latency = completion - arrival."""
-    import torch
-
+    stream one request at a time (FIFO); latency = completion - arrival.
+    The server also runs the stream with every request in FP64, to separate
+    the engine's gain from the precision mix."""
     import hlanc_gb300 as H
     from hlanc_gb300 import build
     build.build()
-    reqs = serve_requests(args.serve_count)
+    reqs = serve_requests(args.serve_count, n_hi=args.serve_nmax)
     for r in reqs:
         prec = H.HLANC_PREC_FP32_REFINE if r["mixed"] else H.HLANC_PREC_FP64
         r["op"] = H.dcsrmv_operator_gpu(r["m"], precision=prec)
@@ -331,39 +331,46 @@ def run_serve(args):
     for r in reqs[:3]:
         H.solve(r["op"], r["nev"], r["ncv"], tol=1e-10)
 
-    def stats(lat, t_total, ok_pairs):
+    def stats(lat, t_total, ok_pairs, ok):
         lat = np.sort(np.array(lat))
-        return {"requests": len(lat), "seconds": t_total, "eigenpairs_per_s": ok_pairs / t_total,
+        return {"requests": len(lat), "converged": ok, "seconds": t_total, "eigenpairs_per_s": ok_pairs / t_total,
                 "p50_s": float(np.percentile(lat, 50)), "p95_s": float(np.percentile(lat, 95)),
                 "p99_s": float(np.percentile(lat, 99))}
 
-    # server
-    srv = H.Server(mem_budget_bytes=150 << 30, max_slots=args.serve_slots)
-    t0 = time.perf_counter()
-    nxt, ids, done, lat, pairs = 0, {}, set(), [], 0
-    while len(done) < len(reqs):
-        now = time.perf_counter() - t0
-        while nxt < len(reqs) and reqs[nxt]["t"] <= now:
-            r = reqs[nxt]
-            kw = dict(tol=1e-10, precision=H.HLANC_PREC_FP32_REFINE if r["mixed"] else H.HLANC_PREC_FP64)
-            ids[srv.submit(r["op"], r["nev"], r["ncv"], **kw)] = nxt
-            nxt += 1
-        active, waiting = srv.step()
-        for rid, i in list(ids.items()):
-            if i in done:
-                continue
-            res = srv.poll(rid)
-            if res is not None:
-                done.add(i)
-                lat.append(time.perf_counter() - t0 - reqs[i]["t"])
-                pairs += reqs[i]["nev"] if res[0] == 0 else 0
-        if active == 0 and waiting == 0 and nxt < len(reqs):
-            time.sleep(max(0.0, reqs[nxt]["t"] - (time.perf_counter() - t0)))
-    served = stats(lat, time.perf_counter() - t0, pairs)
-    srv.close()
+    def serve(all_fp64):
+        srv = H.Server(mem_budget_bytes=150 << 30, max_slots=args.serve_slots, lanes=args.serve_lanes)
+        t0 = time.perf_counter()
+        nxt, ids, done, lat, pairs, ok = 0, {}, set(), [], 0, 0
+        while len(done) < len(reqs):
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and reqs[nxt]["t"] <= now:
+                r = reqs[nxt]
+                mixed = r["mixed"] and not all_fp64
+                kw = dict(tol=1e-10, precision=H.HLANC_PREC_FP32_REFINE if mixed else H.HLANC_PREC_FP64)
+                ids[srv.submit(r["op"], r["nev"], r["ncv"], **kw)] = nxt
+                nxt += 1
+            active, waiting = srv.step()
+            for rid, i in list(ids.items()):
+                if i in done:
+                    continue
+                res = srv.poll(rid)
+                if res is not None:
+                    done.add(i)
+                    lat.append(time.perf_counter() - t0 - reqs[i]["t"])
+                    pairs += reqs[i]["nev"] if res[0] == 0 else 0
+                    ok += res[0] == 0
+            if active == 0 and waiting == 0 and nxt < len(reqs):
+                time.sleep(max(0.0, reqs[nxt]["t"] - (time.perf_counter() - t0)))
+        out = stats(lat, time.perf_counter() - t0, pairs, ok)
+        out["engine"] = srv.stats()
+        srv.close()
+        return out
+
+    served = serve(False)
+    served_fp64 = serve(True)
     # plain FP64, one at a time, FIFO over the same arrivals
     t0 = time.perf_counter()
-    lat, pairs = [], 0
+    lat, pairs, ok = [], 0, 0
     for r in reqs:
         now = time.perf_counter() - t0
         if r["t"] > now:
@@ -371,15 +378,18 @@ def run_serve(args):
         rc, _, _, _ = H.solve(r["op"], r["nev"], r["ncv"], tol=1e-10)
         lat.append(time.perf_counter() - t0 - r["t"])
         pairs += r["nev"] if rc == 0 else 0
-    plain = stats(lat, time.perf_counter() - t0, pairs)
+        ok += rc == 0
+    plain = stats(lat, time.perf_counter() - t0, pairs, ok)
     line = {"metric": "serving throughput (eigenpairs/s) and latency", "value": served["eigenpairs_per_s"],
             "unit": "eigenpairs/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64 (70% fp32 SpMV)",
             "data": "synthetic (seeded generators)",
             "config": {"workload": f"serve{args.serve_count}", "arrivals": "Poisson, mean 200 req/s, seed 4",
-                       "n": "log-uniform [1000, 200000]", "nev": "{4,8,16}, ncv = 3 nev", "mix": "70% fp32+refine",
-                       "slots": args.serve_slots, "mem_budget_GB": 150},
-            "server": served, "plain_fp64_one_at_a_time": plain,
+                       "n": f"log-uniform [1000, {args.serve_nmax}]", "nev": "{4,8,16}, ncv = 3 nev",
+                       "mix": "70% fp32+refine", "tol": 1e-10, "max_restarts": 200,
+                       "slots": args.serve_slots, "lanes": args.serve_lanes or 2, "mem_budget_GB": 150},
+            "server": served, "server_all_fp64": served_fp64, "plain_fp64_one_at_a_time": plain,
             "throughput_ratio": served["eigenpairs_per_s"] / plain["eigenpairs_per_s"],
+            "throughput_ratio_all_fp64": served_fp64["eigenpairs_per_s"] / plain["eigenpairs_per_s"],
             "p99_ratio_plain_over_server": plain["p99_s"] / served["p99_s"]}
     print(json.dumps(line), flush=True)
 
@@ -407,6 +417,8 @@ def main():
     ap.add_argument("--serve", action="store_true", help="serving form (Poisson request stream)")
     ap.add_argument("--serve-count", type=int, default=100)
     ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serve-lanes", type=int, default=0, help="server launch lanes (0 = library default)")
+    ap.add_argument("--serve-nmax", type=int, default=200000, help="largest n of the request stream")
     args = ap.parse_args()
     if args.batch:
         run_batch(args)

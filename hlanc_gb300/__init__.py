@@ -69,7 +69,17 @@ class Profile(C.Structure):
 
 
 class ServerOpts(C.Structure):
-    _fields_ = [("mem_budget_bytes", C.c_size_t), ("max_slots", C.c_int), ("dev", C.c_int)]
+    _fields_ = [("mem_budget_bytes", C.c_size_t), ("max_slots", C.c_int), ("dev", C.c_int), ("lanes", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("steps", C.c_longlong), ("cycles", C.c_longlong), ("admitted", C.c_longlong),
+                ("retired", C.c_longlong), ("wall_ms", C.c_double), ("wait_ms", C.c_double),
+                ("host_ms", C.c_double), ("launch_ms", C.c_double), ("admin_ms", C.c_double),
+                ("gpu_ms", C.c_double), ("reserved", C.c_double * 6)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 HOST_OP = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double))
@@ -112,6 +122,7 @@ def _declare(L):
         "hlanc_server_step": (_i, [_p, _ip, _ip]),
         "hlanc_server_poll": (_i, [_p, C.c_longlong, _ip, _ip, _p, _p, C.POINTER(Stats)]),
         "hlanc_server_cancel": (_i, [_p, C.c_longlong]),
+        "hlanc_server_stats": (_i, [_p, C.POINTER(ServerStats)]),
         "hlanc_server_destroy": (_i, [_p]),
     }
     for name, (res, args) in sig.items():
@@ -409,10 +420,11 @@ class Batch:
 class Server:
     """Continuous batching of eigen-solves (hlanc_server_*): requests are
     admitted by slot count and device-memory budget, every resident solve
-    advances one restart cycle per step(), finished solves are retired."""
+    advances one restart cycle per step(), finished solves are retired.
+    The residents are spread over `lanes` streams (0 = the library default)."""
 
-    def __init__(self, mem_budget_bytes: int, max_slots: int, dev: int = 0):
-        so = ServerOpts(mem_budget_bytes, max_slots, dev)
+    def __init__(self, mem_budget_bytes: int, max_slots: int, dev: int = 0, lanes: int = 0):
+        so = ServerOpts(mem_budget_bytes, max_slots, dev, lanes)
         h = C.c_void_p()
         _check(lib().hlanc_server_create(C.byref(so), C.byref(h)), "hlanc_server_create")
         self._h, self.dev = h, dev
@@ -433,6 +445,9 @@ class Server:
     def poll(self, rid: int):
         n, nev, ncv = self._req[rid]
         done, status = _i(), _i()
+        _check(lib().hlanc_server_poll(self._h, rid, C.byref(done), C.byref(status), None, None, None), "poll")
+        if not done.value:
+            return None
         values = np.zeros(ncv)
         vectors = np.zeros((n, ncv), order="F")
         st = Stats()
@@ -444,6 +459,11 @@ class Server:
 
     def cancel(self, rid: int) -> None:
         _check(lib().hlanc_server_cancel(self._h, rid), "cancel")
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().hlanc_server_stats(self._h, C.byref(st)), "hlanc_server_stats")
+        return st.as_dict()
 
     def close(self):
         if getattr(self, "_h", None) and _lib is not None:

@@ -184,6 +184,8 @@ struct ProbRes {
     size_t bytes = 0;
     int cycles = 0;            // restart cycles launched
     bool live = false;         // resources allocated
+    cudaMemPool_t pool = nullptr;        // stream-ordered allocations (serving) when set
+    cudaStream_t pool_stream = nullptr;
     // host mirror (host restart)
     std::vector<double> h, ritz_s, bnds_s, Q, values;
     State hs;
@@ -200,7 +202,17 @@ struct ProbRes {
         return b;
     }
 
+    cudaError_t dmalloc(void **ptr, size_t b, cudaStream_t s) {
+        return pool ? cudaMallocFromPoolAsync(ptr, b, pool, s) : cudaMalloc(ptr, b);
+    }
+    void dfree(void *ptr) {
+        if (!ptr) return;
+        if (pool) cudaFreeAsync(ptr, pool_stream);
+        else cudaFree(ptr);
+    }
+
     int alloc(cudaStream_t s) {
+        pool_stream = s;
         ld = (n + ROW_ALIGN - 1) / ROW_ALIGN * ROW_ALIGN;
         tr = tile_rows_for(n);
         ntiles = (n + tr - 1) / tr;
@@ -208,7 +220,7 @@ struct ProbRes {
         pstride = (ncv + 2 + 1) & ~1;
         const size_t nd = (size_t)ld * ncv + 2 * (size_t)ld + (size_t)(ntiles + ngroups) * pstride + SM_SIZE(ncv);
         bytes = nd * sizeof(double);
-        CK(cudaMalloc(&block, bytes));
+        CK(dmalloc((void **)&block, bytes, s));
         live = true;
         CK(cudaMemsetAsync(block, 0, bytes, s));
         V = block;
@@ -219,13 +231,13 @@ struct ProbRes {
         small = gpart + (size_t)ngroups * pstride;
         const size_t sb = 512 + 4 * ((size_t)ngroups + 1);
         void *sp = nullptr;
-        CK(cudaMalloc(&sp, sb));
+        CK(dmalloc(&sp, sb, s));
         CK(cudaMemsetAsync(sp, 0, sb, s));
         st = (State *)sp;
         counter = (unsigned *)((char *)sp + 512);
         bytes += sb;
         if (fp32) {
-            CK(cudaMalloc(&x32, (size_t)ld * sizeof(float)));
+            CK(dmalloc((void **)&x32, (size_t)ld * sizeof(float), s));
             CK(cudaMemsetAsync(x32, 0, (size_t)ld * sizeof(float), s));
             bytes += (size_t)ld * sizeof(float);
         }
@@ -236,11 +248,18 @@ struct ProbRes {
         values.assign(ncv, 0.0);
         return HLANC_OK;
     }
+    // Ritz-vector output owned by the problem (ld x ncv)
+    int alloc_vout(cudaStream_t s) {
+        CK(dmalloc((void **)&vout, sizeof(double) * (size_t)ld * ncv, s));
+        own_vout = true;
+        ldo = ld;
+        return HLANC_OK;
+    }
     void release() {
-        if (block) cudaFree(block);
-        if (st) cudaFree(st);
-        if (x32) cudaFree(x32);
-        if (own_vout && vout) cudaFree(vout);
+        dfree(block);
+        dfree(st);
+        dfree(x32);
+        if (own_vout) dfree(vout);
         block = nullptr; st = nullptr; x32 = nullptr; vout = nullptr; own_vout = false;
         live = false;
     }
@@ -273,6 +292,7 @@ public:
     bool own_stream = false;
     bool use_graphs = true;
     bool device_restart = false;
+    cudaMemPool_t pool = nullptr;        // when set, problems allocate from it on `stream`
     std::vector<ProbRes> probs;
     std::vector<int> active;             // problems in the launch tables, in slot order
     Problem *P_d = nullptr;
@@ -334,6 +354,7 @@ public:
         ProbRes p;
         p.n = n; p.ncv = ncv; p.nev0 = nev; p.csr = csr; p.host_op = host_op; p.host_ctx = host_ctx;
         p.fp32 = fp32;
+        p.pool = pool;
         int rc = p.alloc(stream);
         if (rc) { p.release(); return rc == HLANC_ERR_CUDA ? HLANC_ERR_ALLOC : rc; }
         State S = initial_state(nev, ncv, o);
@@ -483,9 +504,20 @@ public:
     // mirrors; with `only`, just those problems (a finalisation must not
     // overwrite the restart decisions of problems still running).
     int pull_mailbox(const std::vector<int> *only = nullptr) {
-        CK(cudaMemcpyAsync(mbox_h, mbox_d, sizeof(double) * mbox_used, cudaMemcpyDeviceToHost, stream));
+        int rc = pull_async();
+        if (rc) return rc;
         CK(cudaStreamSynchronize(stream));
         CK(cudaGetLastError());
+        unpack_mailbox(only);
+        return HLANC_OK;
+    }
+    // Device mailbox -> pinned host copy, ordered after the cycle on `stream`.
+    int pull_async() {
+        CK(cudaMemcpyAsync(mbox_h, mbox_d, sizeof(double) * mbox_used, cudaMemcpyDeviceToHost, stream));
+        return HLANC_OK;
+    }
+    // Host copy of the mailbox -> the problems' State/h mirrors.
+    void unpack_mailbox(const std::vector<int> *only = nullptr) {
         for (size_t a = 0; a < active.size(); ++a) {
             if (only && std::find(only->begin(), only->end(), active[a]) == only->end()) continue;
             ProbRes &p = probs[active[a]];
@@ -493,7 +525,6 @@ public:
             memcpy(&p.hs, slot, sizeof(State));
             if (!device_restart) memcpy(p.h.data(), slot + MBOX_STATE, sizeof(double) * 2 * p.ncv);
         }
-        return HLANC_OK;
     }
 
     // One restart cycle of every active device-operator problem.
@@ -754,6 +785,29 @@ __global__ void k_sum_columns(const double *__restrict__ Y, int ld, int n, int k
 
 int map_status(int st) { return st == ST_CONVERGED ? HLANC_OK : HLANC_NOT_CONVERGED; }
 
+// Mixed precision: the FP32-SpMV phase stops at a relative tolerance of
+// 1e-6 (FP32 rounding of the SpMV sits near 1e-7) and gets a quarter of the
+// restart budget; the FP64 phase then has the whole budget.
+hlanc_opts_t fp32_phase_opts(const hlanc_opts_t &o) {
+    hlanc_opts_t o1 = o;
+    o1.tol = std::max(o.tol > 0 ? o.tol : 0.0, 1e-6);
+    const int mr = o.max_restarts > 0 ? o.max_restarts : 200;
+    o1.max_restarts = std::max(1, mr / 4);
+    return o1;
+}
+
+// Start vector of the FP64 phase, written into r0: the sum of the FP32
+// phase's Ritz vectors when it converged (they are in vout), else that
+// phase's current first Lanczos vector V[:, 0] -- the start vector its
+// restarts have filtered so far.
+void fp64_phase_start(const ProbRes &p, cudaStream_t s) {
+    if (p.hs.status == ST_CONVERGED && p.hs.fin == 2)
+        k_sum_columns<<<304, 256, 0, s>>>(p.vout, p.ldo, p.n, p.hs.nconv, p.r0);
+    else
+        k_sum_columns<<<304, 256, 0, s>>>(p.V, p.ld, p.n, 1, p.r0);
+    launch_counter() += 1;
+}
+
 // Full solve of one problem.  values/vectors are host (device_out = false)
 // or device pointers.
 int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors, int ldv, bool device_out,
@@ -772,8 +826,7 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
     if (rc) return rc;
     const bool fp32 = csr && o.precision == HLANC_PREC_FP32_REFINE && csr->val32_d;
     int idx = 0;
-    hlanc_opts_t o1 = o;
-    if (fp32) o1.tol = std::max(o.tol > 0 ? o.tol : 0.0, 1e-6);   // FP32 phase: loose tolerance
+    const hlanc_opts_t o1 = fp32 ? fp32_phase_opts(o) : o;
     rc = E.add(n, nev, ncv, csr, host_op, host_ctx, fp32 ? 1 : 0, o1, &idx);
     if (rc) return rc;
     E.active = {idx};
@@ -786,20 +839,15 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
     int refine_restarts = 0;
     State S = S1;
     if (fp32) {
-        // FP64 phase warm-started from the sum of the FP32 Ritz vectors
-        const bool warm = S1.status == ST_CONVERGED;
-        if (warm) {
-            if ((rc = E.finalize(idx))) return rc;
-            k_sum_columns<<<304, 256, 0, E.stream>>>(p.vout, p.ldo, p.n, S1.nconv, p.r0);
-            launch_counter() += 1;
-        }
+        // FP64 phase warm-started from the FP32 phase
+        if (S1.status == ST_CONVERGED && (rc = E.finalize(idx))) return rc;
+        fp64_phase_start(p, E.stream);
         State S0 = initial_state(nev, ncv, o);
         p.hs = S0;
         p.cycles = 0;
         CK(cudaMemcpyAsync(p.st, &S0, sizeof S0, cudaMemcpyHostToDevice, E.stream));
         p.fp32 = 0;
         if ((rc = E.upload())) return rc;
-        if (!warm && (rc = E.start_vector(idx, o))) return rc;
         if ((rc = E.norm_init())) return rc;
         if ((rc = drive(E))) return rc;
         S = p.hs;
@@ -1186,7 +1234,7 @@ struct hlanc_batch_s {
 namespace {
 
 // Drive a set of problems; with FP32 operators, a second FP64 phase starts
-// each from the sum of its FP32 Ritz vectors (or a fresh start vector).
+// each from its FP32 phase (fp64_phase_start).
 int run_problems(Engine &E, const std::vector<int> &idx, const std::vector<int> &nev, const std::vector<int> &ncv,
                  const hlanc_opts_t &o, bool fp32, std::vector<State> &first_phase) {
     int rc;
@@ -1205,24 +1253,14 @@ int run_problems(Engine &E, const std::vector<int> &idx, const std::vector<int> 
     if (!conv.empty() && (rc = E.finalize_many(conv))) return rc;
     for (size_t q = 0; q < idx.size(); ++q) {
         ProbRes &p = E.probs[idx[q]];
-        if (p.hs.status == ST_CONVERGED) {
-            k_sum_columns<<<304, 256, 0, E.stream>>>(p.vout, p.ldo, p.n, p.hs.nconv, p.r0);
-            launch_counter() += 1;
-        }
-        const bool warm = p.hs.status == ST_CONVERGED;
+        fp64_phase_start(p, E.stream);
         State S0 = initial_state(nev[q], ncv[q], o);
         p.hs = S0;
         p.cycles = 0;
         p.fp32 = 0;
         CK(cudaMemcpyAsync(p.st, &S0, sizeof S0, cudaMemcpyHostToDevice, E.stream));
-        if (!warm) p.cycles = -1;   // marks "needs a fresh start vector"
     }
     if ((rc = E.upload())) return rc;
-    for (int p : idx)
-        if (E.probs[p].cycles == -1) {
-            E.probs[p].cycles = 0;
-            if ((rc = E.start_vector(p, o))) return rc;
-        }
     if ((rc = E.norm_init())) return rc;
     return drive(E);
 }
@@ -1242,8 +1280,7 @@ int hlanc_batch_create(int dev, int nprob, const hlanc_csr_t *ops, const int *ne
     int rc = b->E.init(dev, b->o.stream, b->o.use_graphs != 0, b->o.restart_on_device != 0);
     if (rc) return rc;
     const bool fp32 = b->o.precision == HLANC_PREC_FP32_REFINE;
-    hlanc_opts_t o1 = b->o;
-    if (fp32) o1.tol = std::max(b->o.tol > 0 ? b->o.tol : 0.0, 1e-6);
+    const hlanc_opts_t o1 = fp32 ? fp32_phase_opts(b->o) : b->o;
     for (int i = 0; i < nprob; ++i) {
         hlanc_csr_s *c = ops[i];
         if (!c || c->dev != dev) return HLANC_ERR_INVALID;
@@ -1332,43 +1369,325 @@ int hlanc_batch_destroy(hlanc_batch_t b) {
 }  // extern "C"
 
 // ---- serving: continuous batching --------------------------------------------------
+// Resident solves are spread over lanes.  A lane is an Engine with its own
+// stream, launch tables and mailbox, so a step can finish one lane's cycle on
+// the host (restart decisions, finalisation, retirement, admission) while the
+// other lanes' cycles run on the device, then launch that lane's next cycle
+// without waiting for it.  Ritz vectors of a converged solve are computed in
+// its lane's next cycle; problem memory comes from a stream-ordered pool, so
+// admitting and retiring solves never synchronises the device.
 struct hlanc_server_s {
     struct Request {
         long long id = 0;
         hlanc_csr_s *csr = nullptr;
         int nev = 0, ncv = 0;
         hlanc_opts_t o;
-        int state = 0;           // 0 pending, 1 active, 2 done
+        int state = 0;             // 0 pending, 1 resident, 2 done
         int status = HLANC_OK;
-        int prob = -1;
+        int lane = -1, prob = -1;
         size_t bytes = 0;
+        double work = 0.0;         // n * ncv, balances the lanes
         bool cancel = false;
-        std::vector<double> values, vectors;
+        bool fresh = false;        // start vector pending
+        bool need_norm = false;    // start-vector norm pending
+        bool push_state = false;   // host State must reach the device (phase switch)
+        bool finishing = false;    // finalised on the host; Ritz vectors in the next cycle
+        std::vector<double> values, vectors, Q2, start;
         hlanc_stats_t stats;
         double t_submit = 0, t_admit = 0, t_done = 0;
-        std::vector<double> start;
-        int phase = 0;           // 1: FP32-SpMV phase of a mixed-precision solve, 0: FP64
-        State first;             // counters of the FP32 phase
+        int phase = 0;             // 1: FP32-SpMV phase of a mixed-precision solve, 0: FP64
+        State first;               // counters of the FP32 phase
+    };
+    struct Lane {
+        Engine E;
+        std::vector<long long> ids;      // resident requests, in slot order
+        bool inflight = false, dirty = true;
+        double work = 0.0;
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     };
     hlanc_server_opts_t opts;
-    Engine E;
+    cudaMemPool_t pool = nullptr;
+    std::vector<std::unique_ptr<Lane>> lanes;
     std::map<long long, Request> reqs;
     std::deque<long long> pending;
-    std::vector<long long> active;   // request ids, engine problems in E.active
+    int resident = 0;
     size_t used = 0;
     long long next_id = 1;
+    hlanc_server_stats_t st;
     std::mutex mu;
+
+    ~hlanc_server_s() {
+        for (auto &L : lanes) {
+            if (L->E.stream) cudaStreamSynchronize(L->E.stream);
+            if (L->ev0) cudaEventDestroy(L->ev0);
+            if (L->ev1) cudaEventDestroy(L->ev1);
+        }
+        lanes.clear();                    // frees go to the pool on the lane streams
+        if (pool) cudaMemPoolDestroy(pool);   // released once those frees complete
+    }
 };
+
+namespace {
+
+using Srv = hlanc_server_s;
+
+// Record a request's result and retire its problem (not its slot in L.ids).
+void srv_finish(Srv &s, Srv::Lane &L, Srv::Request &r, int status) {
+    ProbRes &p = L.E.probs[r.prob];
+    State S = p.hs;
+    int refine = 0;
+    const bool mixed = r.o.precision == HLANC_PREC_FP32_REFINE;
+    if (mixed) {
+        refine = S.iter;
+        S.spmv += r.first.spmv; S.passes += r.first.passes; S.sumc += r.first.sumc;
+        S.sumnev += r.first.sumnev; S.napply += r.first.napply;
+    }
+    r.status = status;
+    fill_stats(&r.stats, S, p, (double)r.csr->nnz, mixed, refine, 0.0, status);
+    r.t_done = now_s();
+    r.stats.seconds = r.t_done - r.t_submit;
+    r.state = 2;
+    L.E.retire(r.prob);
+    s.used -= r.bytes;
+    s.resident -= 1;
+    L.work -= r.work;
+    L.dirty = true;
+    s.st.retired += 1;
+}
+
+// FP32 phase over: the FP64 phase starts from it (fp64_phase_start).
+void srv_switch_to_fp64(Srv::Lane &L, Srv::Request &r) {
+    ProbRes &p = L.E.probs[r.prob];
+    r.first = p.hs;
+    fp64_phase_start(p, L.E.stream);
+    p.hs = initial_state(r.nev, r.ncv, r.o);
+    p.cycles = 0;
+    p.fp32 = 0;
+    r.phase = 0;
+    r.push_state = true;
+    r.need_norm = true;
+    L.dirty = true;                       // the descriptor drops its FP32 values
+}
+
+// Wait for the lane's cycle, then make every decision it enables.
+int srv_complete(Srv &s, Srv::Lane &L) {
+    if (!L.inflight) return HLANC_OK;
+    Engine &E = L.E;
+    double t = now_s();
+    CK(cudaEventSynchronize(L.ev1));
+    CK(cudaGetLastError());
+    s.st.wait_ms += (now_s() - t) * 1e3;
+    L.inflight = false;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, L.ev0, L.ev1) == cudaSuccess) s.st.gpu_ms += ms;
+    E.unpack_mailbox();
+    for (int pi : E.active) E.probs[pi].cycles += 1;
+    s.st.cycles += 1;
+    t = now_s();
+    // Ritz vectors that the cycle produced
+    std::vector<long long> keep;
+    for (long long id : L.ids) {
+        Srv::Request &r = s.reqs[id];
+        ProbRes &p = E.probs[r.prob];
+        if (!r.finishing) { keep.push_back(id); continue; }
+        r.finishing = false;
+        if (p.hs.fin != 2) {                       // not produced: report, do not guess
+            srv_finish(s, L, r, HLANC_ERR_CUDA);
+            continue;
+        }
+        if (r.phase == 1) {
+            srv_switch_to_fp64(L, r);
+            keep.push_back(id);
+            continue;
+        }
+        const int n = p.n, m = p.ncv;
+        r.values.assign(p.values.begin(), p.values.begin() + p.hs.nconv);
+        r.vectors.resize((size_t)n * m);
+        CK(cudaMemcpy2DAsync(r.vectors.data(), sizeof(double) * n, p.vout, sizeof(double) * p.ldo,
+                             sizeof(double) * n, m, cudaMemcpyDeviceToHost, E.stream));
+        CK(cudaStreamSynchronize(E.stream));
+        srv_finish(s, L, r, HLANC_OK);
+    }
+    L.ids.swap(keep);
+    // restart decisions of the problems that extended (slots of the last launch)
+    int running, nev_max, np_max;
+    E.host_restarts(&running, &nev_max, &np_max);
+    // terminal states
+    keep.clear();
+    for (long long id : L.ids) {
+        Srv::Request &r = s.reqs[id];
+        ProbRes &p = E.probs[r.prob];
+        if (r.cancel) {
+            srv_finish(s, L, r, HLANC_ERR_CANCELLED);
+            continue;
+        }
+        if (p.hs.status == ST_RUNNING || r.finishing || r.push_state) { keep.push_back(id); continue; }
+        if (p.hs.status == ST_CONVERGED && p.hs.fin == 0) {
+            host::FinalizeIO io;
+            io.ncv = p.ncv; io.nev0 = p.hs.nev0; io.np0 = p.hs.np0; io.nconv = p.hs.nconv;
+            io.tol = p.hs.tol; io.eps23 = p.hs.eps23;
+            io.h = p.h.data(); io.ritz_s = p.ritz_s.data(); io.bnds_s = p.bnds_s.data();
+            io.values = p.values.data();
+            r.Q2.assign((size_t)p.ncv * p.ncv, 0.0);
+            io.Q2 = r.Q2.data();
+            if (host::finalize(io) == 0) {
+                p.hs.fin = 1;
+                r.finishing = true;
+                keep.push_back(id);
+                continue;
+            }
+            p.hs.status = ST_FAILED;
+        }
+        if (r.phase == 1) {                        // FP32 phase did not converge
+            srv_switch_to_fp64(L, r);
+            keep.push_back(id);
+            continue;
+        }
+        srv_finish(s, L, r, map_status(p.hs.status));
+    }
+    L.ids.swap(keep);
+    s.st.host_ms += (now_s() - t) * 1e3;
+    return HLANC_OK;
+}
+
+// Admit pending requests into lane li while slots and memory allow and no
+// other lane carries less work.
+int srv_admit(Srv &s, int li) {
+    Srv::Lane &L = *s.lanes[li];
+    while (!s.pending.empty() && s.resident < s.opts.max_slots) {
+        Srv::Request &r = s.reqs[s.pending.front()];
+        if (r.cancel) {
+            r.state = 2; r.status = HLANC_ERR_CANCELLED; r.t_done = now_s();
+            s.pending.pop_front();
+            continue;
+        }
+        if (s.used + r.bytes > s.opts.mem_budget_bytes) break;
+        bool lighter_elsewhere = false;
+        for (size_t o = 0; o < s.lanes.size(); ++o)
+            if ((int)o != li && s.lanes[o]->work < L.work) lighter_elsewhere = true;
+        if (lighter_elsewhere) break;
+        const hlanc_opts_t o1 = r.phase == 1 ? fp32_phase_opts(r.o) : r.o;
+        int idx = 0, rc;
+        if ((rc = L.E.add(r.csr->nrows, r.nev, r.ncv, r.csr, nullptr, nullptr, r.phase, o1, &idx))) return rc;
+        if ((rc = L.E.probs[idx].alloc_vout(L.E.stream))) return rc;
+        r.prob = idx;
+        r.lane = li;
+        r.state = 1;
+        r.t_admit = now_s();
+        r.fresh = true;
+        r.need_norm = true;
+        s.used += r.bytes;
+        s.resident += 1;
+        L.work += r.work;
+        L.ids.push_back(r.id);
+        L.dirty = true;
+        s.pending.pop_front();
+        s.st.admitted += 1;
+    }
+    return HLANC_OK;
+}
+
+// Enqueue the lane's next cycle; returns without waiting for it.
+int srv_launch(Srv &s, Srv::Lane &L) {
+    Engine &E = L.E;
+    if (L.ids.empty()) return HLANC_OK;
+    double t = now_s();
+    int rc;
+    if (L.dirty) {
+        E.active.clear();
+        for (long long id : L.ids) E.active.push_back(s.reqs[id].prob);
+        if ((rc = E.upload())) return rc;
+        L.dirty = false;
+    }
+    s.st.admin_ms += (now_s() - t) * 1e3;
+    t = now_s();
+    // mailbox of this cycle, from the host mirrors
+    int steps = 0, basis_nev = 0;
+    bool ritz = false, norm = false;
+    for (size_t a = 0; a < L.ids.size(); ++a) {
+        Srv::Request &r = s.reqs[L.ids[a]];
+        ProbRes &p = E.probs[r.prob];
+        const int m = p.ncv;
+        double *slot = E.mbox_h + E.off_h[a];
+        E.flag_h[a] = 0;
+        if (r.finishing) {
+            memcpy(slot, &p.hs, sizeof(State));
+            memcpy(slot + MBOX_STATE + 2 * m, r.Q2.data(), sizeof(double) * m * m);
+            memcpy(slot + MBOX_STATE + 2 * m + (size_t)m * m, p.values.data(), sizeof(double) * m);
+            E.flag_h[a] = 3;
+            ritz = true;
+        } else if (r.push_state) {
+            memcpy(slot, &p.hs, sizeof(State));
+            E.flag_h[a] = 2;
+            r.push_state = false;
+        } else if (p.cycles > 0 && p.hs.status == ST_RUNNING && p.hs.phase == PH_APPLY) {
+            memcpy(slot, &p.hs, sizeof(State));
+            memcpy(slot + MBOX_STATE, p.h.data(), sizeof(double) * 2 * m);
+            memcpy(slot + MBOX_STATE + 2 * m, p.Q.data(), sizeof(double) * m * m);
+            E.flag_h[a] = 1;
+        }
+        if (p.hs.status == ST_RUNNING) {
+            steps = std::max(steps, p.cycles == 0 ? p.ncv : p.ncv - p.nev0);
+            if (p.cycles > 0 && p.hs.phase == PH_APPLY) basis_nev = std::max(basis_nev, p.hs.nev);
+        }
+    }
+    if ((rc = E.push_mailbox())) return rc;
+    CK(cudaEventRecord(L.ev0, E.stream));
+    const int na = (int)E.active.size();
+    launch_scatter(E.P_d, na, E.off_d, E.flag_d, E.mbox_d, E.stream);
+    for (long long id : L.ids) {
+        Srv::Request &r = s.reqs[id];
+        if (r.fresh) {
+            hlanc_opts_t o = r.o;
+            if (!r.start.empty()) o.start = r.start.data();
+            if ((rc = E.start_vector(r.prob, o))) return rc;
+            r.fresh = false;
+        }
+        norm = norm || r.need_norm;
+        r.need_norm = false;
+    }
+    if (norm) launch_norm_init(E.P_d, E.T_d, E.ntiles, E.stream);
+    if (ritz) launch_ritz(E.P_d, E.T_d, E.ntiles, E.max_ncv, E.stream);
+    if (basis_nev > 0) launch_basis(E.P_d, E.T_d, E.ntiles, E.max_ncv, Engine::basis_bucket(basis_nev), E.stream);
+    for (int k = 0; k < steps; ++k)
+        launch_step(E.P_d, E.T_d, E.ntiles, E.S_d, E.nstiles, k, E.fp32_any, false, E.stream);
+    launch_gather(E.P_d, na, E.off_d, E.mbox_d, E.stream);
+    if ((rc = E.pull_async())) return rc;
+    CK(cudaEventRecord(L.ev1, E.stream));
+    CK(cudaGetLastError());
+    L.inflight = true;
+    s.st.launch_ms += (now_s() - t) * 1e3;
+    return HLANC_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
 int hlanc_server_create(const hlanc_server_opts_t *opts, hlanc_server_t *out) {
-    if (!opts || !out || opts->max_slots <= 0) return HLANC_ERR_INVALID;
+    if (!opts || !out || opts->max_slots <= 0 || opts->lanes < 0 || opts->lanes > 8) return HLANC_ERR_INVALID;
     std::unique_ptr<hlanc_server_s> s(new hlanc_server_s());
     s->opts = *opts;
+    if (s->opts.lanes == 0) s->opts.lanes = 2;
+    memset(&s->st, 0, sizeof s->st);
     DevGuard g(opts->dev);
-    int rc = s->E.init(opts->dev, nullptr, false, false);   // eager launches: the active set changes every tick
-    if (rc) return rc;
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof props);
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = opts->dev;
+    CK(cudaMemPoolCreate(&s->pool, &props));
+    unsigned long long keep_all = ~0ULL;      // keep freed blocks for the next admissions
+    CK(cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep_all));
+    for (int i = 0; i < s->opts.lanes; ++i) {
+        std::unique_ptr<hlanc_server_s::Lane> L(new hlanc_server_s::Lane());
+        int rc = L->E.init(opts->dev, nullptr, false, false);   // the active set changes often: eager launches
+        if (rc) return rc;
+        L->E.pool = s->pool;
+        CK(cudaEventCreate(&L->ev0));
+        CK(cudaEventCreate(&L->ev1));
+        s->lanes.push_back(std::move(L));
+    }
     *out = s.release();
     return HLANC_OK;
 }
@@ -1393,6 +1712,7 @@ int hlanc_server_submit(hlanc_server_t s, hlanc_csr_t csr, int nev, int ncv, con
     r.o.precision = fp32 ? HLANC_PREC_FP32_REFINE : HLANC_PREC_FP64;
     r.phase = fp32 ? 1 : 0;
     r.bytes = ProbRes::estimate(csr->nrows, ncv, fp32 ? 1 : 0);
+    r.work = (double)csr->nrows * ncv;
     if (r.bytes > s->opts.mem_budget_bytes) return HLANC_ERR_ALLOC;
     r.t_submit = now_s();
     memset(&r.stats, 0, sizeof r.stats);
@@ -1402,158 +1722,26 @@ int hlanc_server_submit(hlanc_server_t s, hlanc_csr_t csr, int nev, int ncv, con
     return HLANC_OK;
 }
 
-// One scheduler tick: admit what fits, run one restart cycle of every
-// resident solve (their launches share one sequence), retire finished ones.
+// One scheduler step: every lane completes its cycle in flight, admits what
+// fits and launches its next cycle.  While the host works on one lane, the
+// other lanes' cycles run on the device.
 int hlanc_server_step(hlanc_server_t s, int *n_active, int *n_pending) {
     if (!s) return HLANC_ERR_INVALID;
     std::lock_guard<std::mutex> lk(s->mu);
     DevGuard g(s->opts.dev);
-    Engine &E = s->E;
+    const double t0 = now_s();
     int rc;
-    // cancellations
-    for (auto it = s->active.begin(); it != s->active.end();) {
-        auto &r = s->reqs[*it];
-        if (r.cancel) {
-            E.retire(r.prob);
-            s->used -= r.bytes;
-            r.state = 2; r.status = HLANC_ERR_CANCELLED; r.t_done = now_s();
-            it = s->active.erase(it);
-        } else {
-            ++it;
-        }
+    for (size_t li = 0; li < s->lanes.size(); ++li) {
+        hlanc_server_s::Lane &L = *s->lanes[li];
+        if ((rc = srv_complete(*s, L))) return rc;
+        double t = now_s();
+        if ((rc = srv_admit(*s, (int)li))) return rc;
+        s->st.admin_ms += (now_s() - t) * 1e3;
+        if ((rc = srv_launch(*s, L))) return rc;
     }
-    // admission by slots and memory budget (CSR resident already; basis + workspace)
-    std::vector<long long> admitted;
-    while (!s->pending.empty() && (int)s->active.size() < s->opts.max_slots) {
-        auto &r = s->reqs[s->pending.front()];
-        if (r.cancel) {
-            r.state = 2; r.status = HLANC_ERR_CANCELLED; r.t_done = now_s();
-            s->pending.pop_front();
-            continue;
-        }
-        if (s->used + r.bytes > s->opts.mem_budget_bytes) break;
-        int idx = 0;
-        hlanc_opts_t o1 = r.o;
-        if (r.phase == 1) o1.tol = std::max(r.o.tol > 0 ? r.o.tol : 0.0, 1e-6);   // FP32 phase tolerance
-        if ((rc = E.add(r.csr->nrows, r.nev, r.ncv, r.csr, nullptr, nullptr, r.phase, o1, &idx))) return rc;
-        r.prob = idx;
-        r.state = 1;
-        r.t_admit = now_s();
-        s->used += r.bytes;
-        s->active.push_back(r.id);
-        admitted.push_back(r.id);
-        s->pending.pop_front();
-    }
-    if (s->active.empty()) {
-        if (n_active) *n_active = 0;
-        if (n_pending) *n_pending = (int)s->pending.size();
-        return HLANC_OK;
-    }
-    // launch tables: active problems in request order; keep mailbox state
-    std::vector<State> keep;
-    E.active.clear();
-    for (long long id : s->active) E.active.push_back(s->reqs[id].prob);
-    if ((rc = E.upload())) return rc;
-    // restarts decided at the previous tick are re-armed in the mailbox
-    for (size_t a = 0; a < E.active.size(); ++a) {
-        ProbRes &p = E.probs[E.active[a]];
-        E.flag_h[a] = 0;
-        if (p.cycles > 0 && p.hs.status == ST_RUNNING && p.hs.phase == PH_APPLY) {
-            double *slot = E.mbox_h + E.off_h[a];
-            memcpy(slot, &p.hs, sizeof(State));
-            memcpy(slot + MBOX_STATE, p.h.data(), sizeof(double) * 2 * p.ncv);
-            memcpy(slot + MBOX_STATE + 2 * p.ncv, p.Q.data(), sizeof(double) * p.ncv * p.ncv);
-            E.flag_h[a] = 1;
-        }
-    }
-    for (long long id : admitted) {
-        auto &r = s->reqs[id];
-        hlanc_opts_t o = r.o;
-        if (!r.start.empty()) o.start = r.start.data();
-        if ((rc = E.start_vector(r.prob, o))) return rc;
-    }
-    if (!admitted.empty() && (rc = E.norm_init())) return rc;
-    int steps = 0, basis_nev = 0;
-    for (int pi : E.active) {
-        ProbRes &p = E.probs[pi];
-        steps = std::max(steps, p.cycles == 0 ? p.ncv : p.ncv - p.nev0);
-        if (p.cycles > 0 && p.hs.phase == PH_APPLY) basis_nev = std::max(basis_nev, p.hs.nev);
-    }
-    if ((rc = E.run_cycle(steps, basis_nev))) return rc;
-    int running, nev_max, np_max;
-    E.host_restarts(&running, &nev_max, &np_max);
-    // retire finished solves
-    std::vector<int> conv;
-    for (long long id : s->active) {
-        auto &r = s->reqs[id];
-        ProbRes &p = E.probs[r.prob];
-        if (p.hs.status != ST_RUNNING && p.hs.status == ST_CONVERGED) conv.push_back(r.prob);
-    }
-    if (!conv.empty() && (rc = E.finalize_many(conv))) return rc;
-    // a finished FP32 phase becomes an FP64 solve started from the sum of its
-    // Ritz vectors (or from a fresh start vector if it did not converge)
-    bool need_norm = false;
-    for (long long id : s->active) {
-        auto &r = s->reqs[id];
-        ProbRes &p = E.probs[r.prob];
-        if (r.phase != 1 || p.hs.status == ST_RUNNING) continue;
-        r.first = p.hs;
-        const bool warm = p.hs.status == ST_CONVERGED;
-        if (warm) {
-            k_sum_columns<<<304, 256, 0, E.stream>>>(p.vout, p.ldo, p.n, p.hs.nconv, p.r0);
-            launch_counter() += 1;
-        }
-        State S0 = initial_state(r.nev, r.ncv, r.o);
-        p.hs = S0;
-        p.cycles = 0;
-        p.fp32 = 0;
-        CK(cudaMemcpyAsync(p.st, &S0, sizeof S0, cudaMemcpyHostToDevice, E.stream));
-        r.phase = 0;
-        need_norm = true;
-        if (!warm) {
-            E.active.clear();
-            for (long long q : s->active) E.active.push_back(s->reqs[q].prob);
-            if ((rc = E.upload())) return rc;
-            hlanc_opts_t o = r.o;
-            if (!r.start.empty()) o.start = r.start.data();
-            if ((rc = E.start_vector(r.prob, o))) return rc;
-        }
-    }
-    if (need_norm) {
-        E.active.clear();
-        for (long long q : s->active) E.active.push_back(s->reqs[q].prob);
-        if ((rc = E.upload())) return rc;
-        if ((rc = E.norm_init())) return rc;
-    }
-    for (auto it = s->active.begin(); it != s->active.end();) {
-        auto &r = s->reqs[*it];
-        ProbRes &p = E.probs[r.prob];
-        if (p.hs.status == ST_RUNNING) { ++it; continue; }
-        r.status = map_status(p.hs.status);
-        if (p.hs.status == ST_CONVERGED) {
-            const int n = p.n, m = p.ncv;
-            r.values.assign(p.values.begin(), p.values.begin() + p.hs.nconv);
-            r.vectors.resize((size_t)n * m);
-            CK(cudaMemcpy2DAsync(r.vectors.data(), sizeof(double) * n, p.vout, sizeof(double) * p.ldo,
-                                 sizeof(double) * n, m, cudaMemcpyDeviceToHost, E.stream));
-            CK(cudaStreamSynchronize(E.stream));
-        }
-        State S = p.hs;
-        int refine = 0;
-        if (r.o.precision == HLANC_PREC_FP32_REFINE) {
-            refine = S.iter;
-            S.spmv += r.first.spmv; S.passes += r.first.passes; S.sumc += r.first.sumc;
-            S.sumnev += r.first.sumnev; S.napply += r.first.napply;
-        }
-        fill_stats(&r.stats, S, p, (double)r.csr->nnz, r.o.precision == HLANC_PREC_FP32_REFINE, refine, 0.0, r.status);
-        r.t_done = now_s();
-        r.stats.seconds = r.t_done - r.t_submit;
-        r.state = 2;
-        E.retire(r.prob);
-        s->used -= r.bytes;
-        it = s->active.erase(it);
-    }
-    if (n_active) *n_active = (int)s->active.size();
+    s->st.steps += 1;
+    s->st.wall_ms += (now_s() - t0) * 1e3;
+    if (n_active) *n_active = s->resident;
     if (n_pending) *n_pending = (int)s->pending.size();
     return HLANC_OK;
 }
@@ -1580,6 +1768,13 @@ int hlanc_server_cancel(hlanc_server_t s, long long request_id) {
     auto it = s->reqs.find(request_id);
     if (it == s->reqs.end()) return HLANC_ERR_INVALID;
     if (it->second.state != 2) it->second.cancel = true;
+    return HLANC_OK;
+}
+
+int hlanc_server_stats(hlanc_server_t s, hlanc_server_stats_t *out) {
+    if (!s || !out) return HLANC_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->st;
     return HLANC_OK;
 }
 

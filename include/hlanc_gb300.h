@@ -178,10 +178,27 @@ int hlanc_batch_destroy(hlanc_batch_t b);
 typedef struct hlanc_server_s *hlanc_server_t;
 
 typedef struct {
-    size_t mem_budget_bytes;  /* admission budget: CSR + basis + workspace */
+    size_t mem_budget_bytes;  /* admission budget: basis + workspace + Ritz output */
     int max_slots;            /* problems resident at once */
     int dev;
+    int lanes;                /* launch lanes (streams) the residents are spread over;
+                                 0 = 2.  A step finishes one lane's restart cycle on the
+                                 host while the other lanes' cycles run on the device. */
 } hlanc_server_opts_t;
+
+/* Scheduler counters since creation (times in milliseconds). */
+typedef struct {
+    long long steps;          /* hlanc_server_step calls */
+    long long cycles;         /* lane restart cycles completed */
+    long long admitted, retired;
+    double wall_ms;           /* inside hlanc_server_step */
+    double wait_ms;           /* host blocked on a lane's cycle */
+    double host_ms;           /* restart decisions, finalisation, result copies */
+    double launch_ms;         /* enqueueing device work */
+    double admin_ms;          /* admission, launch tables */
+    double gpu_ms;            /* device spans of the lane cycles (overlapping lanes add up) */
+    double reserved[6];
+} hlanc_server_stats_t;
 
 int hlanc_server_create(const hlanc_server_opts_t *opts, hlanc_server_t *out);
 /* Submit a solve on an existing device operator; returns a request id. */
@@ -194,6 +211,7 @@ int hlanc_server_step(hlanc_server_t s, int *active, int *pending);
 int hlanc_server_poll(hlanc_server_t s, long long request_id, int *done, int *status,
                       double *values, double *vectors, hlanc_stats_t *stats);
 int hlanc_server_cancel(hlanc_server_t s, long long request_id);
+int hlanc_server_stats(hlanc_server_t s, hlanc_server_stats_t *out);
 int hlanc_server_destroy(hlanc_server_t s);
 
 /* ---- diagnostics ---------------------------------------------------------- */
