@@ -505,9 +505,22 @@ def main():
     f1.record(stream)
     torch.cuda.synchronize()
     spmv_ms = f0.elapsed_time(f1) / reps
+    # the same with L2 flushed (a 256 MB write) before each call, timed one by one
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    flushed = []
+    for rep in range(8):
+        with torch.cuda.stream(stream):
+            flush.fill_(rep)
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        op.spmv_async(xs.data_ptr(), ys.data_ptr(), stream.cuda_stream)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        flushed.append(g0.elapsed_time(g1))
+    spmv_flushed_ms = statistics.median(flushed[2:])
     nnz_g = op.nnz_general()
     spmv_bytes = 12.0 * nnz_g + 4.0 * (m.n + 1) + 16.0 * m.n
-    del xs, ys
+    del xs, ys, flush
 
     # roofline: one profiled solve
     pst = solve_dev(profile=True)
@@ -545,8 +558,11 @@ def main():
             "spmv": {"us_per_call": spmv_ms * 1e3, "bytes_per_call": spmv_bytes,
                      "achieved_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9,
                      "frac_of_hbm": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / measured_peaks()[0],
-                     "note": "FP64 CSR SpMV alone, algorithmic bytes 12 nnz + 4(n+1) + 16 n, x/y not L2-flushed "
-                             "(x is 8n bytes of L2-resident gather)"}}
+                     "us_per_call_l2_flushed": spmv_flushed_ms * 1e3,
+                     "frac_of_hbm_l2_flushed": spmv_bytes / (spmv_flushed_ms * 1e-3) / 1e9 / measured_peaks()[0],
+                     "note": "FP64 CSR SpMV alone, algorithmic bytes 12 nnz + 4(n+1) + 16 n; back-to-back calls "
+                             "(the CSR arrays exceed L2, x/y may stay in it) and, separately, each call after a "
+                             "256 MB L2 flush"}}
     if rank == 0 and world == 1 and not args.no_cpu:
         full = FULL_SOLVE_SPMV.get(args.workload) or stats[-1]["spmv_calls"]
         line["cpu_baseline"] = cpu_sample(m, wl, os.cpu_count() or 1, full)
