@@ -304,6 +304,7 @@ public:
     bool device_restart = false;
     cudaMemPool_t pool = nullptr;        // when set, problems allocate from it on `stream`
     int min_tile_rows = 128;
+    bool basis_tc = true;                // basis update on the tensor cores when the shape fits
     std::vector<ProbRes> probs;
     std::vector<int> active;             // problems in the launch tables, in slot order
     Problem *P_d = nullptr;
@@ -497,7 +498,7 @@ public:
     void enqueue_cycle(int steps, int basis_nev) {
         const int na = (int)active.size();
         if (!device_restart) launch_scatter(P_d, na, off_d, flag_d, mbox_d, stream);
-        if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), stream);
+        if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), basis_tc, stream);
         for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, stream);
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
@@ -583,7 +584,7 @@ public:
         if (rc) return rc;
         const int na = (int)active.size();
         if (!device_restart) launch_scatter(P_d, na, off_d, flag_d, mbox_d, stream);
-        if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), stream);
+        if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), basis_tc, stream);
         const int k = p.hs.k;
         for (int s = 0; s < steps; ++s) {
             const int j = k + s;
@@ -836,6 +837,7 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
     Engine E;
     int rc = E.init(dev, o.stream, o.use_graphs != 0, o.restart_on_device != 0);
     if (rc) return rc;
+    E.basis_tc = o.basis_kernel != HLANC_BASIS_FP64;
     const bool fp32 = csr && o.precision == HLANC_PREC_FP32_REFINE && csr->val32_d;
     int idx = 0;
     const hlanc_opts_t o1 = fp32 ? fp32_phase_opts(o) : o;
@@ -949,6 +951,7 @@ void hlanc_opts_default(hlanc_opts_t *o) {
     o->use_graphs = 1;
     o->restart_on_device = 0;
     o->profile = 0;
+    o->basis_kernel = HLANC_BASIS_AUTO;
 }
 
 int hlanc_last_profile(hlanc_profile_t *out) {
@@ -1291,6 +1294,7 @@ int hlanc_batch_create(int dev, int nprob, const hlanc_csr_t *ops, const int *ne
     DevGuard g(dev);
     int rc = b->E.init(dev, b->o.stream, b->o.use_graphs != 0, b->o.restart_on_device != 0);
     if (rc) return rc;
+    b->E.basis_tc = b->o.basis_kernel != HLANC_BASIS_FP64;
     if (nprob > 1) b->E.min_tile_rows = BATCH_MIN_TILE_ROWS;
     const bool fp32 = b->o.precision == HLANC_PREC_FP32_REFINE;
     const hlanc_opts_t o1 = fp32 ? fp32_phase_opts(b->o) : b->o;
@@ -1661,7 +1665,8 @@ int srv_launch(Srv &s, Srv::Lane &L) {
     }
     if (norm) launch_norm_init(E.P_d, E.T_d, E.ntiles, E.stream);
     if (ritz) launch_ritz(E.P_d, E.T_d, E.ntiles, E.max_ncv, E.stream);
-    if (basis_nev > 0) launch_basis(E.P_d, E.T_d, E.ntiles, E.max_ncv, Engine::basis_bucket(basis_nev), E.stream);
+    if (basis_nev > 0)
+        launch_basis(E.P_d, E.T_d, E.ntiles, E.max_ncv, Engine::basis_bucket(basis_nev), E.basis_tc, E.stream);
     for (int k = 0; k < steps; ++k)
         launch_step(E.P_d, E.T_d, E.ntiles, E.S_d, E.nstiles, k, E.fp32_any, false, E.stream);
     launch_gather(E.P_d, na, E.off_d, E.mbox_d, E.stream);

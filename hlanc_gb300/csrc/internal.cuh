@@ -233,8 +233,11 @@ void launch_prep_f32(const Problem *P_d, const Tile *tiles_d, int ntiles, int st
 void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, double *xout,
                      cudaStream_t s);
 void launch_restart(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
+// tensor_cores: use k_basis_tc (kernels_tc.cu) when the shape fits it.
 void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, int max_nev,
-                  cudaStream_t s);
+                  bool tensor_cores, cudaStream_t s);
+bool basis_tc_fits(int max_ncv, int nev_max);
+void launch_basis_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, int nev_max, cudaStream_t s);
 void launch_finalize(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
 void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, cudaStream_t s);
 void launch_spmv(const int *row_ptr, const int *col, const double *val, const SpmvTile *stiles, int nstiles,

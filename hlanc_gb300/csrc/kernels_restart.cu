@@ -665,7 +665,11 @@ static void basis_t(const Problem *P_d, const Tile *tiles_d, int ntiles, int max
 // nev is rounded up to a multiple of 4: the unrolled output loop issues no
 // FP64 instruction for more than 3 absent columns.
 void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, int max_nev,
-                  cudaStream_t s) {
+                  bool tensor_cores, cudaStream_t s) {
+    if (tensor_cores && basis_tc_fits(max_ncv, max_nev)) {
+        launch_basis_tc(P_d, tiles_d, ntiles, max_nev, s);
+        return;
+    }
     switch ((max_nev + 3) / 4) {
     case 0: case 1: basis_t<4>(P_d, tiles_d, ntiles, max_ncv, s); break;
     case 2: basis_t<8>(P_d, tiles_d, ntiles, max_ncv, s); break;

@@ -1,0 +1,482 @@
+// kernels_tc.cu -- the restart's basis update V[:, 0:nev) <- V Q on the
+// fifth-generation tensor cores (tcgen05), accurate to FP64 level.
+//
+// GB300 runs FP64 FMAs at 2 per clock per SM on the CUDA cores, so the
+// FP64 form of this update (k_basis: ~nev + np FMAs per output) is
+// FP64-bound.  Here the product is computed exactly in integer arithmetic
+// on the bf16 tensor pipe (the splitting idea of Ozaki et al., "Error-free
+// transformations of matrix multiplication by using fast routines of matrix
+// multiplication", Numer. Algorithms 2012):
+//
+//  * every row r of the 128-row block of V gets the exponent E_r of its
+//    largest element; each element becomes the integer |X| = |v| 2^(55-E_r)
+//    (truncated, < 2^55) with the element's sign, i.e. 7 unsigned 8-bit
+//    digits a_0 (most significant) .. a_6, each stored as a signed bf16
+//    (exact: |digit| <= 255 needs 8 significand bits);
+//  * every output column i of Q (the band of Q[:, i], i < nev, and the
+//    residual column Q[:, nev]) is split the same way with its own exponent;
+//  * D_L = sum over s + t = L of A_s B_t (L = 0..6) accumulates in FP32 in
+//    tensor memory.  Digit products are < 2^16 and K <= 64, so a pair sum is
+//    < 2^22 and levels 0..3 (at most 4 pairs) stay below 2^24: exact.  The
+//    lower levels can round by a few units at weights 2^-32 .. 2^-48 of
+//    level 0, i.e. below FP64 precision.  Levels past 6 are dropped
+//    (weight <= 2^-56 of the result's scale).
+//  * the levels are recombined per output in 64-bit integers and two
+//    FP64 conversions: 4 FP64 instructions per output instead of ~50 FMAs.
+//
+// Shapes: M = 128 rows per MMA, N = padded nev + 1 (<= 64), K = ncv padded
+// to 16 (<= 64).  Operands live in shared memory in the no-swizzle K-major
+// layout (8-row x 16-byte core matrices); the accumulators (7 x N columns)
+// in tensor memory.  One CTA per tile of rows, one CTA per SM.
+#include <cuda_bf16.h>
+
+#include "internal.cuh"
+
+namespace hlanc {
+
+namespace tc {
+
+constexpr int BM = 128;       // rows per block = MMA M
+constexpr int NDIG = 7;       // digit planes / levels
+constexpr int KMAX = 64;      // largest padded ncv
+constexpr int NMAX = 64;      // largest padded nev + 1
+constexpr int THREADS = 256;
+constexpr unsigned SPIN_LIMIT = 1u << 20;   // MMA completion wait (far above any real wait)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor, no swizzle: start, leading byte offset
+// (next core matrix along K), stride byte offset (next 8 rows), version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: D f32, A/B bf16, both K-major.
+__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                    uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(mbar))
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint64_t *m, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *m, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(m)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Levels 0..6 of 4 consecutive outputs of this thread's TMEM lane: seven
+// 32x32b.x4 loads (level L at column offset L * npad) and one wait, in one
+// asm block so the registers are read only after the wait.
+__device__ __forceinline__ void tmem_ld_levels4(uint32_t a, uint32_t npad, float (&d)[NDIG][4]) {
+    uint32_t r[NDIG * 4];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%28];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%4,%5,%6,%7}, [%29];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%8,%9,%10,%11}, [%30];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%12,%13,%14,%15}, [%31];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%32];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%20,%21,%22,%23}, [%33];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%24,%25,%26,%27}, [%34];\n\t"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27])
+        : "r"(a), "r"(a + npad), "r"(a + 2 * npad), "r"(a + 3 * npad), "r"(a + 4 * npad), "r"(a + 5 * npad),
+          "r"(a + 6 * npad)
+        : "memory");
+#pragma unroll
+    for (int L = 0; L < NDIG; ++L)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) d[L][e] = __uint_as_float(r[L * 4 + e]);
+}
+
+// Start streaming rows [r0, r0 + rows) of the first m columns of V into L2
+// (one bulk prefetch per column, issued by threads 0..m-1).  V's columns
+// are 512-byte aligned and at least an even number of rows long past any
+// tile row, so rows is rounded up to an even count (16-byte multiple).
+__device__ __forceinline__ void prefetch_rows_l2(const double *V, size_t ld, int m, int r0, int rows) {
+    const int k = threadIdx.x;
+    if (rows <= 0 || k >= m) return;
+    const unsigned bytes = (unsigned)(((rows + 1) & ~1) * 8);
+    const double *p = V + r0 + (size_t)k * ld;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Byte offset of element (row, k) in a no-swizzle K-major operand with
+// kpad columns: core matrix (row/8, k/8) at (row/8)*SBO + (k/8)*128,
+// SBO = (kpad/8)*128; inside, row%8 at 16 B, k%8 at 2 B.
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k, int kpad) {
+    return (uint32_t)((row >> 3) * (kpad >> 3) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// Biased exponent field of a double (0 for zero and subnormals).
+__device__ __forceinline__ int exp_field(double x) {
+    return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+// The 7 digits of one element, relative to the largest biased exponent emax
+// of its row / column, as bf16 pairs: digits of 8 elements -> 7 x uint4.
+// |X| = (mantissa << 2) >> (emax - e) < 2^55; digit s = byte (6 - s) of |X|.
+__device__ __forceinline__ void split8(const double (&x)[8], int emax, uint4 (&planes)[NDIG]) {
+    float dg[NDIG][8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(x[e]);
+        const int ex = (int)((bits >> 52) & 0x7FF);
+        unsigned long long mag = 0ull;
+        if (ex != 0) {
+            const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+            const int sh = emax - ex;
+            mag = sh < 64 ? (mant << 2) >> sh : 0ull;
+        }
+        const unsigned lo = (unsigned)mag, hi = (unsigned)(mag >> 32);
+        const bool neg = (bits >> 63) != 0ull;
+        const unsigned top = neg ? 0xCB000000u : 0x4B000000u;   // +-(2^23 + byte)
+        const float c23 = neg ? -8388608.0f : 8388608.0f;
+        // digit s = byte (6 - s): bytes 0..3 of lo, 4..6 of hi
+        dg[6][e] = __uint_as_float(__byte_perm(lo, top, 0x7540)) - c23;
+        dg[5][e] = __uint_as_float(__byte_perm(lo, top, 0x7541)) - c23;
+        dg[4][e] = __uint_as_float(__byte_perm(lo, top, 0x7542)) - c23;
+        dg[3][e] = __uint_as_float(__byte_perm(lo, top, 0x7543)) - c23;
+        dg[2][e] = __uint_as_float(__byte_perm(hi, top, 0x7540)) - c23;
+        dg[1][e] = __uint_as_float(__byte_perm(hi, top, 0x7541)) - c23;
+        dg[0][e] = __uint_as_float(__byte_perm(hi, top, 0x7542)) - c23;
+    }
+#pragma unroll
+    for (int s = 0; s < NDIG; ++s) {
+        __nv_bfloat162 p0 = __floats2bfloat162_rn(dg[s][0], dg[s][1]);
+        __nv_bfloat162 p1 = __floats2bfloat162_rn(dg[s][2], dg[s][3]);
+        __nv_bfloat162 p2 = __floats2bfloat162_rn(dg[s][4], dg[s][5]);
+        __nv_bfloat162 p3 = __floats2bfloat162_rn(dg[s][6], dg[s][7]);
+        planes[s].x = *reinterpret_cast<unsigned *>(&p0);
+        planes[s].y = *reinterpret_cast<unsigned *>(&p1);
+        planes[s].z = *reinterpret_cast<unsigned *>(&p2);
+        planes[s].w = *reinterpret_cast<unsigned *>(&p3);
+    }
+}
+
+// Levels D_0..D_6 (exact integers in FP32) of one output -> the FP64 value
+// (hi 2^32 + lo) 2^S with hi = D_0 2^16 + D_1 2^8 + D_2, lo = D_3 2^24 +
+// D_4 2^16 + D_5 2^8 + D_6 and S = ex + fx - 2106 (ex, fx: the biased
+// exponents the row and the column were split against).  Both halves are
+// placed exactly into doubles by adding them to the significand of
+// 1.5 * 2^(84+S) resp. 1.5 * 2^(52+S) (|hi|, |lo| < 2^51), so the value
+// costs three FP64 additions with one rounding.
+__device__ __forceinline__ double combine(const float (&d)[NDIG], int ex, int fx) {
+    // every level is an integer below 2^26 in magnitude
+    const long long l0 = __float2int_rn(d[0]), l1 = __float2int_rn(d[1]), l2 = __float2int_rn(d[2]);
+    const long long l3 = __float2int_rn(d[3]), l4 = __float2int_rn(d[4]), l5 = __float2int_rn(d[5]);
+    const long long l6 = __float2int_rn(d[6]);
+    const long long hi = (l0 << 16) + (l1 << 8) + l2;                 // |hi| < 2^41
+    const long long lo = (l3 << 24) + (l4 << 16) + (l5 << 8) + l6;    // |lo| < 2^50
+    const int S = ex + fx - 2106;
+    const long long eA = 1023 + 84 + S, eB = 1023 + 52 + S;           // biased exponents of the carriers
+    if (eB >= 1 && eA <= 2046) {
+        const long long half = 1LL << 51;                             // 1.5 = 1 + 2^-1
+        const double A = __longlong_as_double((eA << 52) + half + hi);
+        const double B = __longlong_as_double((eB << 52) + half + lo);
+        const double cA = __longlong_as_double((eA << 52) + half);
+        const double cB = __longlong_as_double((eB << 52) + half);
+        return (A - cA) + (B - cB);
+    }
+    return scalbn(fma((double)hi, 4294967296.0, (double)lo), S);
+}
+
+}  // namespace tc
+
+// One CTA per tile; 128-row blocks of the tile in turn.
+template <int NPAD>
+__global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__restrict__ probs,
+                                                            const Tile *__restrict__ tiles) {
+    using namespace tc;
+    const Tile t = tiles[blockIdx.x];
+    const Problem &P = probs[t.prob];
+    State *S = P.st;
+    if (S->status != ST_RUNNING || S->phase != PH_APPLY) return;
+    const int m = P.ncv, nev = S->nev, np = S->np;
+    const int kpad = (m + 15) & ~15;
+    const int nout = nev + 1;
+    constexpr uint32_t NCOLS = (NDIG * NPAD > 256) ? 512u : (NDIG * NPAD > 128 ? 256u : 128u);
+
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *sA = smem;                                   // NDIG x BM x kpad bf16
+    // Q's digit planes stacked: rows (t + 6) * NPAD + i hold plane t of output
+    // i (t = 0..6); the six blocks before them are zero.  The B operand of A
+    // plane s is this stack shifted by (6 - s) blocks, so one MMA over
+    // N = 7 * NPAD columns adds plane s's share to every level L at once
+    // (block L of the window is plane L - s, or zero).
+    unsigned char *sB = smem + (size_t)NDIG * BM * KMAX * 2;    // 13 x NPAD x kpad bf16
+    __shared__ uint64_t s_mbar;
+    __shared__ uint32_t s_taddr;
+    __shared__ int s_rowexp[2][BM];
+    __shared__ int s_colexp[NPAD];
+    __shared__ double s_red[32], s_mine[1], s_tot[1];
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const double *Q = P.small + SM_Q(m);
+    const double *h = P.small + SM_H(m);
+    const size_t aplane = (size_t)BM * kpad * 2, bplane = (size_t)NPAD * kpad * 2;
+    for (int i = tid; i < (int)(6 * bplane / 16); i += THREADS)
+        reinterpret_cast<uint4 *>(sB)[i] = make_uint4(0u, 0u, 0u, 0u);
+
+    prefetch_rows_l2(P.V, (size_t)P.ld, m, t.row0, min(BM, t.row1 - t.row0));
+    if (warp == 0) {
+        tmem_alloc(&s_taddr, NCOLS);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        mbar_init(&s_mbar, 1);
+        s_fail = 0;
+    }
+    for (int i = tid; i < NPAD; i += THREADS) s_colexp[i] = 0;
+    __syncthreads();
+
+    // ---- B planes: the output columns of Q, split per column -------------------
+    // column i < nev: Q[k, i] for k <= i + np (the band), i == nev: Q[:, nev]
+    auto qval = [&](int k, int i) -> double {
+        if (i > nev || k >= m) return 0.0;
+        if (i < nev && k > i + np) return 0.0;
+        return Q[k + (size_t)i * m];
+    };
+    const int kg = kpad >> 3;
+    for (int it = tid; it < NPAD * kg; it += THREADS) {
+        const int i = it / kg, g = it % kg;
+        int emax = 0;
+        for (int e = 0; e < 8; ++e) emax = max(emax, exp_field(qval(8 * g + e, i)));
+        atomicMax(&s_colexp[i], emax);
+    }
+    __syncthreads();
+    for (int it = tid; it < NPAD * kg; it += THREADS) {
+        const int i = it / kg, g = it % kg;
+        double x[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) x[e] = qval(8 * g + e, i);
+        uint4 pl[NDIG];
+        split8(x, s_colexp[i], pl);
+        const uint32_t off = kmajor_off(i, 8 * g, kpad);
+#pragma unroll
+        for (int s = 0; s < NDIG; ++s) *reinterpret_cast<uint4 *>(sB + (s + 6) * bplane + off) = pl[s];
+    }
+
+    // N = 7 * NPAD in one MMA, or two (each N <= 256, a multiple of 16)
+    constexpr int NTOT = NDIG * NPAD;
+    constexpr int N1 = NTOT <= 256 ? NTOT : ((NTOT / 2 + 15) / 16) * 16;
+    constexpr int N2 = NTOT - N1;
+    const uint32_t idesc1 = instr_desc(BM, N1), idesc2 = instr_desc(BM, N2 > 0 ? N2 : 16);
+    const uint32_t sbo = (uint32_t)kg * 128u;
+    const uint32_t taddr = s_taddr;
+    const double hn = h[nev];
+    const double qlast = Q[(m - 1) + (size_t)(nev - 1) * m];
+    const double *__restrict__ rin = (m & 1) ? P.r1 : P.r0;
+    double *__restrict__ rout = (nev & 1) ? P.r1 : P.r0;
+    const size_t ld = (size_t)P.ld;
+    double nrm = 0.0;
+    uint32_t phase = 0;
+
+    // loader mapping: row r of the block, groups g0.. of 8 columns
+    const int lr = tid & (BM - 1), half = tid >> 7;
+    const int gper = (kg + 1) >> 1, g0 = half * gper, g1 = min(kg, g0 + gper);
+
+    for (int R0 = t.row0; R0 < t.row1; R0 += BM) {
+        prefetch_rows_l2(P.V, ld, m, R0 + BM, min(BM, t.row1 - (R0 + BM)));
+        // 1. load this thread's part of row R0 + lr and its largest exponent
+        const int row = R0 + lr;
+        const bool rok = row < t.row1;
+        double x[4][8];
+        int emax = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int g = g0 + q;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int k = 8 * g + e;
+                x[q][e] = (rok && g < g1 && k < m) ? P.V[row + (size_t)k * ld] : 0.0;
+                emax = max(emax, exp_field(x[q][e]));
+            }
+        }
+        s_rowexp[half][lr] = emax;
+        __syncthreads();
+        const int ex = max(s_rowexp[0][lr], s_rowexp[1][lr]);
+        // 2. digit planes of the block
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int g = g0 + q;
+            if (g >= g1) break;
+            uint4 pl[NDIG];
+            split8(x[q], ex, pl);
+            const uint32_t off = kmajor_off(lr, 8 * g, kpad);
+#pragma unroll
+            for (int s = 0; s < NDIG; ++s) *reinterpret_cast<uint4 *>(sA + s * aplane + off) = pl[s];
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        // 3. one thread issues the 28 digit-pair products per K step
+        if (tid == 0) {
+            fence_after();
+            const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+            const uint32_t n1_bytes = (uint32_t)(N1 / 8) * sbo;     // N1 rows further in the stack
+            for (int s = 0; s < NDIG; ++s) {
+                const uint32_t bs = b0 + (uint32_t)((6 - s) * bplane);
+                for (int kk = 0; kk < kpad / 16; ++kk) {
+                    const uint64_t ad = smem_desc(a0 + (uint32_t)(s * aplane) + kk * 256u, 128u, sbo);
+                    const uint32_t acc = (s | kk) ? 1u : 0u;
+                    mma(taddr, ad, smem_desc(bs + kk * 256u, 128u, sbo), idesc1, acc);
+                    if (N2 > 0)
+                        mma(taddr + (uint32_t)N1, ad, smem_desc(bs + n1_bytes + kk * 256u, 128u, sbo), idesc2, acc);
+                }
+            }
+            mma_commit(&s_mbar);
+        }
+        // 4. wait for the products (bounded)
+        {
+            unsigned spins = 0;
+            while (!mbar_try_wait(&s_mbar, phase)) {
+                if (++spins > SPIN_LIMIT) {
+                    s_fail = 1;
+                    break;
+                }
+            }
+        }
+        phase ^= 1u;
+        fence_after();
+        __syncthreads();
+        if (s_fail) break;
+        // 5. recombine: warp w reads TMEM lanes 32 (w % 4) .. +31; the two warps of a
+        //    lane quarter take alternate groups of 4 outputs
+        {
+            const int q4 = warp & 3, ch = warp >> 2;
+            const int r = 32 * q4 + lane;
+            const int orow = R0 + r;
+            const bool ok = orow < t.row1;
+            const int exr = max(s_rowexp[0][r], s_rowexp[1][r]);
+            const uint32_t lane_base = taddr + ((uint32_t)(32 * q4) << 16);
+            for (int c0 = ch * 4; c0 < nout; c0 += 8) {
+                float d[NDIG][4];
+                tmem_ld_levels4(lane_base + (uint32_t)c0, (uint32_t)NPAD, d);
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int i = c0 + e;
+                    if (i >= nout || !ok) continue;
+                    float lv[NDIG];
+#pragma unroll
+                    for (int L = 0; L < NDIG; ++L) lv[L] = d[L][e];
+                    const double v = combine(lv, exr, s_colexp[i]);
+                    if (i < nev) {
+                        P.V[orow + (size_t)i * ld] = v;
+                    } else {                                      // residual (HLanc.hpp:1605-1614)
+                        double res = rin[orow] * qlast;
+                        if (hn > 0.0) res = res + hn * v;
+                        rout[orow] = res;
+                        nrm = fma(res, res, nrm);
+                    }
+                }
+            }
+        }
+        fence_before();
+        __syncthreads();
+    }
+
+    // release tensor memory (all TMEM reads are complete)
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        tmem_dealloc(taddr, NCOLS);
+    }
+    if (s_fail) {
+        if (tid == 0) atomicExch(&S->err, 5);
+        return;
+    }
+    nrm = block_sum0(nrm, s_red);
+    if (tid == 0) s_mine[0] = nrm;
+    __syncthreads();
+    if (!finish_tile(P, blockIdx.x - P.tile0, 1, s_mine, s_tot)) return;
+    if (tid == 0) {
+        S->rnorm = sqrt(s_tot[0]);                    // HLanc.hpp:1735
+        S->phase = PH_EXTEND;
+        S->sumnev += nev;
+        S->napply += 1;
+    }
+}
+
+template <int NPAD>
+static size_t basis_tc_smem() {
+    return (size_t)tc::NDIG * tc::BM * tc::KMAX * 2 + (size_t)13 * NPAD * tc::KMAX * 2;
+}
+
+template <int NPAD>
+static void basis_tc_t(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s) {
+    static bool attr = false;
+    const size_t smem = basis_tc_smem<NPAD>();
+    if (!attr) {
+        cudaFuncSetAttribute(k_basis_tc<NPAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = true;
+    }
+    prof_begin(s);
+    k_basis_tc<NPAD><<<ntiles, tc::THREADS, smem, s>>>(P_d, tiles_d);
+    prof_end(KC_BASIS, s);
+    launch_counter() += 1;
+}
+
+// The tensor-core basis update serves problems with ncv <= 64 and
+// nev + 1 <= 64 (nev_max is the engine's bucket of nev, so nev <= 60 in
+// practice); the caller uses k_basis otherwise.
+bool basis_tc_fits(int max_ncv, int nev_max) { return max_ncv <= tc::KMAX && nev_max + 1 <= tc::NMAX; }
+
+void launch_basis_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, int nev_max, cudaStream_t s) {
+    const int nout = nev_max + 1;
+    if (nout <= 16) basis_tc_t<16>(P_d, tiles_d, ntiles, s);
+    else if (nout <= 32) basis_tc_t<32>(P_d, tiles_d, ntiles, s);
+    else if (nout <= 48) basis_tc_t<48>(P_d, tiles_d, ntiles, s);
+    else basis_tc_t<64>(P_d, tiles_d, ntiles, s);
+}
+
+}  // namespace hlanc

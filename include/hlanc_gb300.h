@@ -37,6 +37,11 @@ extern "C" {
 #define HLANC_PREC_FP64           0  /* FP64 SpMV (the reference's arithmetic) */
 #define HLANC_PREC_FP32_REFINE    1  /* FP32 SpMV, FP64 everywhere else, FP64 refinement */
 
+/* Kernel of the restart's basis update V <- V Q (hlanc_opts_t.basis_kernel). */
+#define HLANC_BASIS_AUTO          0  /* tensor cores (FP64-accurate integer splitting) when
+                                        ncv <= 64 and nev <= 60, else the FP64 kernel */
+#define HLANC_BASIS_FP64          1  /* always the FP64 CUDA-core kernel */
+
 /* Largest ncv the device restart kernels accept, and largest nev. */
 #define HLANC_MAX_NCV           128
 #define HLANC_MAX_NEV            63
@@ -101,7 +106,8 @@ typedef struct {
     int use_graphs;           /* replay identical restart cycles as CUDA graphs */
     int restart_on_device;    /* run the O(ncv^2) restart math in a device kernel instead of on the host */
     int profile;              /* time every kernel launch with CUDA events (eager launches); see hlanc_last_profile */
-    int reserved[5];
+    int basis_kernel;         /* HLANC_BASIS_*; default HLANC_BASIS_AUTO */
+    int reserved[4];
 } hlanc_opts_t;
 
 /* Fill defaults (tol 0, max_restarts 200, FP64, seed 0, graphs on, host restart). */

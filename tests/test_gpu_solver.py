@@ -216,6 +216,35 @@ def test_graph_and_eager_agree(H):
     assert s1["spmv_calls"] == s2["spmv_calls"]
 
 
+@pytest.mark.parametrize("gen,nev,ncv", [
+    (lambda: G.laplacian_3d(20, shift_seed=1), 20, 60),        # tensor-core basis (ncv <= 64)
+    (lambda: G.chung_lu_normalized(4096, seed=2), 16, 48),
+    (lambda: G.laplacian_2d(40), 4, 12),
+])
+def test_basis_tensor_cores_agree_with_fp64(H, gen, nev, ncv):
+    # the tensor-core V*Q (FP64-exact integer splitting) and the FP64 kernel
+    # give the same pairs to FP64-level accuracy
+    m = gen()
+    op = H.dcsrmv_operator_gpu(m)
+    rc1, v1, x1, s1 = H.solve(op, nev, ncv, tol=1e-10)
+    rc2, v2, x2, s2 = H.solve(op, nev, ncv, tol=1e-10, basis_fp64=True)
+    assert rc1 == rc2 == 0
+    assert np.abs(v1[:nev] - v2[:nev]).max() <= 1e-12 * np.abs(v2[:nev]).max()
+    _check_pairs(m, v1, x1, nev)
+    assert abs(s1["restarts"] - s2["restarts"]) <= 2
+
+
+def test_basis_fp64_path_beyond_tensor_core_shape(H):
+    # ncv > 64 takes the FP64 kernel under the default setting
+    m = G.laplacian_2d(30)
+    op = H.dcsrmv_operator_gpu(m)
+    rc, vals, vecs, st = H.solve(op, 20, 80, tol=1e-10)
+    assert rc == 0
+    ref = np.sort(np.linalg.eigvalsh(G.to_scipy(m).toarray()))[-20:]
+    assert np.abs(vals[:20] - ref).max() <= EV_RTOL * np.abs(ref).max()
+    _check_pairs(m, vals, vecs, 20)
+
+
 def test_native_library_loaded(H):
     import os
     with open("/proc/self/maps") as f:
