@@ -215,6 +215,11 @@ __device__ __forceinline__ double block_sum0(double v, double *scratch /* >= 32 
     return s;
 }
 
+// Step s of the current extension runs for this problem.
+__device__ __forceinline__ bool step_active(const State *S, int s) {
+    return S->status == ST_RUNNING && S->phase == PH_EXTEND && s < S->np;
+}
+
 __device__ __forceinline__ const double *step_in(const Problem &P, int j) { return (j & 1) ? P.r1 : P.r0; }
 __device__ __forceinline__ double *step_out(const Problem &P, int j) { return (j & 1) ? P.r0 : P.r1; }
 
@@ -237,6 +242,8 @@ void launch_restart(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
 void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, int max_nev,
                   bool tensor_cores, cudaStream_t s);
 bool basis_tc_fits(int max_ncv, int nev_max);
+
+
 void launch_basis_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, int nev_max, cudaStream_t s);
 void launch_finalize(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
 void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, cudaStream_t s);

@@ -65,9 +65,6 @@ __global__ void __launch_bounds__(TPB) k_norm_init(const Problem *__restrict__ p
     }
 }
 
-__device__ __forceinline__ bool step_active(const State *S, int s) {
-    return S->status == ST_RUNNING && S->phase == PH_EXTEND && s < S->np;
-}
 
 // ---- SpMV work units ----------------------------------------------------------------
 // Short rows: thread per row, entries read directly in batches of 8 so eight

@@ -160,33 +160,42 @@ __device__ __forceinline__ int exp_field(double x) {
     return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
 }
 
-// The 7 digits of one element, relative to the largest biased exponent emax
-// of its row / column, as bf16 pairs: digits of 8 elements -> 7 x uint4.
-// |X| = (mantissa << 2) >> (emax - e) < 2^55; digit s = byte (6 - s) of |X|.
+// |X| = (mantissa << 2) >> (emax - e) < 2^55 of one element, relative to the
+// largest biased exponent emax of its row / column, as two words, and its sign.
+__device__ __forceinline__ void split_mag(double x, int emax, unsigned &lo, unsigned &hi, bool &neg) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    unsigned long long mag = 0ull;
+    if (ex != 0) {
+        const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+        const int sh = emax - ex;
+        mag = sh < 64 ? (mant << 2) >> sh : 0ull;
+    }
+    lo = (unsigned)mag;
+    hi = (unsigned)(mag >> 32);
+    neg = (bits >> 63) != 0ull;
+}
+
+// Digit s (0 = most significant) of |X| with the element's sign, as a float:
+// byte (6 - s) placed in the significand of +-(2^23 + byte), minus +-2^23.
+__device__ __forceinline__ float digit_of(unsigned lo, unsigned hi, bool neg, int s) {
+    const unsigned top = neg ? 0xCB000000u : 0x4B000000u;
+    const float c23 = neg ? -8388608.0f : 8388608.0f;
+    const unsigned word = s < 3 ? hi : lo;
+    const unsigned sel = 0x7540u | (unsigned)(s < 3 ? 2 - s : 6 - s);
+    return __uint_as_float(__byte_perm(word, top, sel)) - c23;
+}
+
+// The 7 digits of 8 elements as bf16 pairs: 7 x uint4.
 __device__ __forceinline__ void split8(const double (&x)[8], int emax, uint4 (&planes)[NDIG]) {
     float dg[NDIG][8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
-        const unsigned long long bits = (unsigned long long)__double_as_longlong(x[e]);
-        const int ex = (int)((bits >> 52) & 0x7FF);
-        unsigned long long mag = 0ull;
-        if (ex != 0) {
-            const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-            const int sh = emax - ex;
-            mag = sh < 64 ? (mant << 2) >> sh : 0ull;
-        }
-        const unsigned lo = (unsigned)mag, hi = (unsigned)(mag >> 32);
-        const bool neg = (bits >> 63) != 0ull;
-        const unsigned top = neg ? 0xCB000000u : 0x4B000000u;   // +-(2^23 + byte)
-        const float c23 = neg ? -8388608.0f : 8388608.0f;
-        // digit s = byte (6 - s): bytes 0..3 of lo, 4..6 of hi
-        dg[6][e] = __uint_as_float(__byte_perm(lo, top, 0x7540)) - c23;
-        dg[5][e] = __uint_as_float(__byte_perm(lo, top, 0x7541)) - c23;
-        dg[4][e] = __uint_as_float(__byte_perm(lo, top, 0x7542)) - c23;
-        dg[3][e] = __uint_as_float(__byte_perm(lo, top, 0x7543)) - c23;
-        dg[2][e] = __uint_as_float(__byte_perm(hi, top, 0x7540)) - c23;
-        dg[1][e] = __uint_as_float(__byte_perm(hi, top, 0x7541)) - c23;
-        dg[0][e] = __uint_as_float(__byte_perm(hi, top, 0x7542)) - c23;
+        unsigned lo, hi;
+        bool neg;
+        split_mag(x[e], emax, lo, hi, neg);
+#pragma unroll
+        for (int s = 0; s < NDIG; ++s) dg[s][e] = digit_of(lo, hi, neg, s);
     }
 #pragma unroll
     for (int s = 0; s < NDIG; ++s) {
@@ -478,5 +487,6 @@ void launch_basis_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, int ne
     else if (nout <= 48) basis_tc_t<48>(P_d, tiles_d, ntiles, s);
     else basis_tc_t<64>(P_d, tiles_d, ntiles, s);
 }
+
 
 }  // namespace hlanc
