@@ -114,6 +114,10 @@ def _declare(L):
                              C.POINTER(Stats)]),
         "hlanc_solve_device": (_i, [_i, _i, _i, _i, _p, _p, _i, _p, C.POINTER(Opts), C.POINTER(Stats)]),
         "hlanc_residuals_device": (_i, [_p, _i, _p, _p, _i, _p, _p]),
+        "hlanc_residuals_host": (_i, [_p, _i, _p, _p, _i, _p, _p]),
+        "hlanc_eigs_write": (_i, [C.c_char_p, _i, _i, _p, _p, _i]),
+        "hlanc_eigs_info": (_i, [C.c_char_p, _ip, _ip]),
+        "hlanc_eigs_read": (_i, [C.c_char_p, _p, _p, _i]),
         "hlanc_last_profile": (_i, [C.POINTER(Profile)]),
         "hlanc_diag_fp64_tflops": (_i, [_i, C.POINTER(C.c_double)]),
         "hlanc_batch_create": (_i, [_i, _i, _p, _p, _p, C.POINTER(Opts), C.POINTER(_p)]),
@@ -360,6 +364,39 @@ def residuals_device(op: dcsrmv_operator_gpu, k: int, values_ptr: int, vectors_p
     _check(lib().hlanc_residuals_device(op.handle, k, values_ptr, vectors_ptr, ldv, res.ctypes.data,
                                         rd.ctypes.data), "residuals")
     return res, rd
+
+
+def residuals(op: dcsrmv_operator_gpu, values: np.ndarray, vectors: np.ndarray):
+    """||A v_i - lambda_i v_i|| and verify_eigs' r-diff for host pairs
+    (values[k], vectors n x k), computed on the device."""
+    vals = np.ascontiguousarray(values, dtype=np.float64)
+    vecs = np.asfortranarray(vectors, dtype=np.float64)
+    k = vals.shape[0]
+    res = np.zeros(k)
+    rd = np.zeros(k)
+    _check(lib().hlanc_residuals_host(op.handle, k, vals.ctypes.data, vecs.ctypes.data, vecs.shape[0],
+                                      res.ctypes.data, rd.ctypes.data), "residuals")
+    return res, rd
+
+
+def write_eigs(filename: str, values: np.ndarray, vectors: np.ndarray) -> None:
+    """Eigenpair text file of the reference demo (demo/HLanc_solver_gpu.cu:57-66)."""
+    vals = np.ascontiguousarray(values, dtype=np.float64)
+    vecs = np.asfortranarray(vectors, dtype=np.float64)
+    n = vecs.shape[0]
+    _check(lib().hlanc_eigs_write(filename.encode(), vals.shape[0], n, vals.ctypes.data, vecs.ctypes.data,
+                                  max(n, 1)), "eigs write")
+
+
+def read_eigs(filename: str):
+    """(values[nev], vectors n x nev) from an eigenpair text file (demo/verify_eigs.cu:8-44)."""
+    nev, n = _i(), _i()
+    _check(lib().hlanc_eigs_info(filename.encode(), C.byref(nev), C.byref(n)), "eigs info")
+    vals = np.zeros(nev.value)
+    vecs = np.zeros((n.value, nev.value), order="F")
+    _check(lib().hlanc_eigs_read(filename.encode(), vals.ctypes.data, vecs.ctypes.data, max(n.value, 1)),
+           "eigs read")
+    return vals, vecs
 
 
 def kernel_launches() -> int:

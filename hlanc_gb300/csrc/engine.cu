@@ -924,7 +924,7 @@ const char *hlanc_status_string(int status) {
     case HLANC_ERR_CUDA: return "CUDA error";
     case HLANC_ERR_ALLOC: return "allocation failed";
     case HLANC_ERR_DEVICE_TIMEOUT: return "device wait timed out";
-    case HLANC_ERR_IO: return "matrix file error";
+    case HLANC_ERR_IO: return "file open/parse/write error";
     case HLANC_ERR_UNSUPPORTED: return "unsupported size";
     case HLANC_ERR_CALLBACK: return "host operator failed";
     case HLANC_ERR_CANCELLED: return "cancelled";
@@ -1233,6 +1233,48 @@ int hlanc_residuals_device(hlanc_csr_t csr, int k, const double *values_d, const
     return HLANC_OK;
 }
 
+int hlanc_residuals_host(hlanc_csr_t csr, int k, const double *values_h, const double *vectors_h, int ldv_h,
+                         double *resid_h, double *rdiff_h) {
+    if (!csr || k <= 0 || !values_h || !vectors_h || ldv_h < csr->nrows) return HLANC_ERR_INVALID;
+    DevGuard g(csr->dev);
+    const int n = csr->nrows;
+    double *vals = nullptr, *vecs = nullptr;
+    CK(cudaMalloc(&vals, sizeof(double) * (size_t)k));
+    cudaError_t e = cudaMalloc(&vecs, sizeof(double) * (size_t)n * k);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(vals, values_h, sizeof(double) * k, cudaMemcpyHostToDevice, csr->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(vecs, sizeof(double) * n, vectors_h, sizeof(double) * ldv_h, sizeof(double) * n, k,
+                              cudaMemcpyHostToDevice, csr->stream);
+    int rc = e == cudaSuccess ? hlanc_residuals_device(csr, k, vals, vecs, n, resid_h, rdiff_h) : HLANC_ERR_CUDA;
+    cudaFree(vals);
+    if (vecs) cudaFree(vecs);
+    return rc;
+}
+
+int hlanc_eigs_write(const char *filename, int nev, int n, const double *values, const double *vectors,
+                     int ldv) {
+    return HLanc::write_eigs(filename, nev, n, values, vectors, ldv);
+}
+
+int hlanc_eigs_info(const char *filename, int *nev, int *n) {
+    if (!nev || !n) return HLANC_ERR_INVALID;
+    FILE *fp = filename ? fopen(filename, "r") : nullptr;
+    if (!fp) return HLANC_ERR_IO;
+    const bool ok = fscanf(fp, "%d", nev) == 1 && fscanf(fp, "%d", n) == 1 && *nev >= 0 && *n >= 0;
+    fclose(fp);
+    return ok ? HLANC_OK : HLANC_ERR_IO;
+}
+
+int hlanc_eigs_read(const char *filename, double *values, double *vectors, int ldv) {
+    HLanc::eigs_t e;
+    int rc = e.load(filename);
+    if (rc) return rc;
+    if ((e.nev > 0 && !values) || (e.nev > 0 && e.n > 0 && (!vectors || ldv < e.n))) return HLANC_ERR_INVALID;
+    if (e.nev > 0) memcpy(values, e.value.data(), sizeof(double) * e.nev);
+    for (int c = 0; c < e.nev; ++c)
+        memcpy(vectors + (size_t)c * ldv, e.vector.data() + (size_t)c * e.n, sizeof(double) * e.n);
+    return HLANC_OK;
+}
 
 // ---- batched solves ------------------------------------------------------------------
 }  // extern "C"

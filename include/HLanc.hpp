@@ -378,6 +378,67 @@ protected:
     hlanc_csr_t h;
 };
 
+// ---- eigenpair text files -----------------------------------------------------------
+// The format the reference demo writes (demo/HLanc_solver_gpu.cu:57-66) and its
+// verifier reads (demo/verify_eigs.cu:8-44): nev, n, the nev eigenvalues, then
+// n rows of nev vector entries, every number as "%23.15lE".
+inline int write_eigs(FILE *fp, int nev, int n, double const *values, double const *vectors, int ldv) {
+    if (!fp || nev < 0 || n < 0 || (nev > 0 && (!values || (n > 0 && (!vectors || ldv < n)))))
+        return HLANC_ERR_INVALID;
+    if (fprintf(fp, "%d\n%d\n", nev, n) < 0) return HLANC_ERR_IO;
+    for (int i = 0; i < nev; ++i)
+        if (fprintf(fp, "%23.15lE\n", values[i]) < 0) return HLANC_ERR_IO;
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < nev; ++c)
+            if (fprintf(fp, "%23.15lE%c", vectors[r + (size_t)c * ldv], c + 1 == nev ? '\n' : ' ') < 0)
+                return HLANC_ERR_IO;
+    return HLANC_OK;
+}
+
+inline int write_eigs(char const *filename, int nev, int n, double const *values, double const *vectors, int ldv) {
+    FILE *fp = filename ? fopen(filename, "w") : nullptr;
+    if (!fp) return HLANC_ERR_IO;
+    int rc = write_eigs(fp, nev, n, values, vectors, ldv);
+    if (fclose(fp) != 0 && rc == HLANC_OK) rc = HLANC_ERR_IO;
+    return rc;
+}
+
+// Reader of that format; vectors are stored column-major with ld n.  The
+// constructor exits on errors like the reference demo's eigs_t; load()
+// returns a status instead.
+struct eigs_t {
+    int nev = 0, n = 0;
+    std::vector<double> value, vector;
+
+    eigs_t() = default;
+    explicit eigs_t(char const *filename) {
+        const int rc = load(filename);
+        if (rc != HLANC_OK) {
+            warn("Error reading eigenpairs from \"%s\" (%s).\n", filename, hlanc_status_string(rc));
+            exit(1);
+        }
+    }
+    int load(char const *filename) {
+        FILE *fp = filename ? fopen(filename, "r") : nullptr;
+        if (!fp) return HLANC_ERR_IO;
+        int rc = HLANC_OK;
+        if (fscanf(fp, "%d", &nev) != 1 || fscanf(fp, "%d", &n) != 1 || nev < 0 || n < 0) {
+            rc = HLANC_ERR_IO;
+        } else {
+            value.assign(nev, 0.0);
+            vector.assign((size_t)n * nev, 0.0);
+            for (int i = 0; i < nev && rc == HLANC_OK; ++i)
+                if (fscanf(fp, "%lE", &value[i]) != 1) rc = HLANC_ERR_IO;
+            for (int r = 0; r < n && rc == HLANC_OK; ++r)
+                for (int c = 0; c < nev && rc == HLANC_OK; ++c)
+                    if (fscanf(fp, "%lE", &vector[(size_t)c * n + r]) != 1) rc = HLANC_ERR_IO;
+        }
+        fclose(fp);
+        if (rc != HLANC_OK) { nev = n = 0; value.clear(); vector.clear(); }
+        return rc;
+    }
+};
+
 template <typename T> struct is_device_csr_operator : std::false_type {};
 template <> struct is_device_csr_operator<dcsrmv_operator_gpu> : std::true_type {};
 

@@ -28,7 +28,7 @@ extern "C" {
 #define HLANC_ERR_CUDA            3  /* a CUDA runtime call failed */
 #define HLANC_ERR_ALLOC           4  /* device or host allocation failed / over budget */
 #define HLANC_ERR_DEVICE_TIMEOUT  5  /* a bounded device-side wait expired */
-#define HLANC_ERR_IO              6  /* matrix file open/parse/write error */
+#define HLANC_ERR_IO              6  /* file open/parse/write error (matrix or eigenpair files) */
 #define HLANC_ERR_UNSUPPORTED     7  /* size outside the supported envelope */
 #define HLANC_ERR_CALLBACK        8  /* a host operator callback reported failure */
 #define HLANC_ERR_CANCELLED       9  /* a serving request was cancelled */
@@ -168,6 +168,20 @@ int hlanc_residuals_device(hlanc_csr_t csr, int k, const double *values_d,
 int hlanc_residuals_device_noalloc(hlanc_csr_t csr, int k, const double *values_d,
                                    const double *vectors_d, int ldv_d, double *resid_h,
                                    double *rdiff_h);
+
+/* Same check for pairs in host memory (values[k], vectors ldv x k):
+ * verify_eigs' per-vector r-diff (demo/verify_eigs.cu:52-98) and ||A v - lambda v||. */
+int hlanc_residuals_host(hlanc_csr_t csr, int k, const double *values_h, const double *vectors_h, int ldv_h,
+                         double *resid_h, double *rdiff_h);
+
+/* ---- eigenpair text files (demo/HLanc_solver_gpu.cu:57-66, demo/verify_eigs.cu:8-44)
+ * nev, n, then nev eigenvalues and n rows of nev vector entries, "%23.15lE". */
+int hlanc_eigs_write(const char *filename, int nev, int n, const double *values, const double *vectors,
+                     int ldv);
+/* Sizes of a file (to allocate for hlanc_eigs_read). */
+int hlanc_eigs_info(const char *filename, int *nev, int *n);
+/* values[nev]; vectors ldv x nev (ldv >= n), column-major. */
+int hlanc_eigs_read(const char *filename, double *values, double *vectors, int ldv);
 
 /* ---- batched solves (one launch sequence over many problems) ----------- */
 typedef struct hlanc_batch_s *hlanc_batch_t;

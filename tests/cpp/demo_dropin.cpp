@@ -1,6 +1,8 @@
 // Drop-in check: the reference demo's calls (demo/HLanc_demo.cu,
 // demo/HLanc_solver_gpu.cu) compiled unchanged against include/HLanc.hpp.
-// Usage: demo_dropin <pp-or-mm-or-bin> <matrix file> <nev> <ncv>
+// Usage: demo_dropin <pp-or-mm-or-bin> <matrix file> <nev> <ncv> [eigs file]
+// With an eigs file the first solve's pairs are written in the demo's text
+// format (demo/HLanc_solver_gpu.cu:57-66) and read back (demo/verify_eigs.cu).
 #include <cstdio>
 #include <cstdlib>
 
@@ -26,8 +28,8 @@ template <typename op_t> struct dcsrmv_wrapper_t {
 };
 
 int main(int argc, char *argv[]) {
-    if (argc != 5) {
-        HLanc::warn("Usage: %s <bin|mm|pp> <matrix_file> <nev> <ncv>\n", argv[0]);
+    if (argc != 5 && argc != 6) {
+        HLanc::warn("Usage: %s <bin|mm|pp> <matrix_file> <nev> <ncv> [eigs_file]\n", argv[0]);
         return 2;
     }
     HLanc::dcsr_matrix_t m(argv[1], argv[2]);
@@ -39,6 +41,11 @@ int main(int argc, char *argv[]) {
     printf("device %d", ret);
     for (int i = 0; i < nev; ++i) printf(" %.15e", values[i]);
     printf("\n");
+    if (argc == 6) {
+        if (HLanc::write_eigs(argv[5], nev, n, values, vectors, n) != 0) return 3;
+        HLanc::eigs_t eigs(argv[5]);
+        printf("eigs %d %d %d\n", ret, eigs.nev, eigs.n);
+    }
     // wrapped operator -> host-functor path, like demo/HLanc_solver_gpu.cu
     dcsrmv_wrapper_t<HLanc::dcsrmv_operator_gpu> wrapped(op);
     ret = HLanc::ds_solver_gpu(n, nev, ncv, values, vectors, n, wrapped);

@@ -173,14 +173,36 @@ def test_cpp_dropin_end_to_end(H, tmp_path, readers_golden):
                                       int(g["simple_meta"][1]))
     pp = tmp_path / "simple.pp"
     mat.save_pp(str(pp))
-    out = subprocess.check_output([str(exe), "pp", str(pp), "4", "12"]).decode().splitlines()
+    eigs = tmp_path / "simple.eigs"
+    out = subprocess.check_output([str(exe), "pp", str(pp), "4", "12", str(eigs)]).decode().splitlines()
     ref = golden("simple_pp.npz")["values"]
     for line in out:
         parts = line.split()
         kind, rc = parts[0], int(parts[1])
         assert rc == 0, line
+        if kind == "eigs":
+            assert parts[2:] == ["4", "16"], line
+            continue
         vals = np.array([float(x) for x in parts[-4:]])
         assert np.abs(vals - ref).max() <= 1e-10 * np.abs(ref).max(), line
+    # the demo's eigs file passes the reference verifier's check (demo/verify_eigs.cu)
+    ev, ex = H.read_eigs(str(eigs))
+    op = H.dcsrmv_operator_gpu(mat)
+    res, rd = H.residuals(op, ev, ex)
+    assert rd.max() < 1e-9 and np.abs(ev - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def test_residuals_host_match_device(H, torch):
+    m = G.laplacian_2d(30)
+    op = H.dcsrmv_operator_gpu(m)
+    rc, vals, vecs, st = H.solve(op, 5, 15)
+    assert rc == 0
+    r_h, d_h = H.residuals(op, vals[:5], vecs[:, :5])
+    vd = torch.tensor(vals[:5], dtype=torch.float64, device="cuda")
+    xd = torch.tensor(np.ascontiguousarray(vecs[:, :5].T), dtype=torch.float64, device="cuda")
+    r_d, d_d = H.residuals_device(op, 5, vd.data_ptr(), xd.data_ptr(), m.n)
+    assert np.array_equal(r_h, r_d) and np.array_equal(d_h, d_d)
+    assert r_h.max() < 1e-10 * 8
 
 
 def test_server_mixed_precision_requests(H):
