@@ -64,8 +64,8 @@ struct hlanc_csr_s {
 };
 
 // Split rows into SpMV work units (see SpmvTile): runs of short rows (at most
-// SPMV_ROWS rows / SPMV_NNZ entries), runs of up to TPB/32 medium rows, and
-// single wide rows.
+// SPMV_ROWS rows / SPMV_NNZ entries; thread, 4 or 8 lanes per row by the
+// run's mean length), runs of up to TPB/32 medium rows, and single wide rows.
 static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &out) {
     out.clear();
     auto len = [&](int r) { return (long long)rp[r + 1] - rp[r]; };
@@ -86,7 +86,8 @@ static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &ou
                 nnz += len(r);
                 ++r;
             }
-            out.push_back({0, r0, r, 0});
+            const long long mean = nnz / (r - r0);
+            out.push_back({0, r0, r, mean > SUBWARP8_MEAN ? 4 : (mean > SUBWARP4_MEAN ? 3 : 0)});
         }
     }
 }

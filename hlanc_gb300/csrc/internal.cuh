@@ -92,7 +92,9 @@ struct Tile { int prob, row0, row1, pad; };
 //                    and <= SPMV_NNZ entries in total; thread per row;
 //   kind 1 (medium): up to TPB/32 consecutive rows of LONG_ROW..WIDE_ROW
 //                    entries; warp per row;
-//   kind 2 (wide):   one row of more than WIDE_ROW entries; whole CTA.
+//   kind 2 (wide):   one row of more than WIDE_ROW entries; whole CTA;
+//   kind 3 / 4:      a short-row unit whose mean row length is above
+//                    SUBWARP4_MEAN / SUBWARP8_MEAN: 4 / 8 lanes per row.
 // Balancing by entries keeps skewed (power-law) matrices from piling their
 // long rows onto a few CTAs, and no CTA waits on a barrier for one warp.
 // 1024-row units amortise each CTA's start-up loads (measured 24% faster
@@ -100,6 +102,12 @@ struct Tile { int prob, row0, row1, pad; };
 constexpr int SPMV_ROWS = 1024;
 constexpr int SPMV_NNZ = 16384;
 constexpr int WIDE_ROW = 2048;
+// Measured on GB300 (power-law graph, n = 2^22, median row 18 entries):
+// 4 / 8 lanes per row above a mean of 12 / 32 entries took the standalone
+// SpMV from 828 to 644 us (in the solver 877 -> 776 us); 8/24, 12/20 and
+// 16/- were slower, and the 7-entry Laplacian rows keep thread per row.
+constexpr int SUBWARP4_MEAN = 12;
+constexpr int SUBWARP8_MEAN = 32;
 struct SpmvTile { int prob, row0, row1, kind; };
 
 // ---- device helpers --------------------------------------------------------

@@ -96,6 +96,36 @@ __device__ __forceinline__ void spmv_short(const int *__restrict__ rp, const int
     }
 }
 
+// Short rows of uneven length (power-law graphs): LANES lanes per row, so a
+// warp waits on the longest of 32 / LANES rows instead of 32, and the lanes
+// of a row read its entries contiguously; a shuffle tree sums the row.
+template <typename T, int LANES, typename Emit>
+__device__ __forceinline__ void spmv_subwarp(const int *__restrict__ rp, const int *__restrict__ ci,
+                                             const T *__restrict__ val, const T *__restrict__ x, int row0,
+                                             int row1, Emit emit) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int RPW = 32 / LANES;                 // rows per warp at a time
+    const int q = lane & (LANES - 1);
+    for (int base = row0 + warp * RPW; base < row1; base += (TPB / 32) * RPW) {
+        const int r = base + lane / LANES;
+        T acc = T(0);
+        if (r < row1) {
+            const int a = rp[r], b = rp[r + 1];
+            int i = a + q;
+            for (; i + LANES < b; i += 2 * LANES) {
+                const T v0 = val[i], v1 = val[i + LANES];
+                const T x0 = x[ci[i]], x1 = x[ci[i + LANES]];
+                acc = fma(v0, x0, acc);
+                acc = fma(v1, x1, acc);
+            }
+            if (i < b) acc = fma(val[i], x[ci[i]], acc);
+        }
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (q == 0 && r < row1) emit(r, acc);
+    }
+}
+
 // Medium rows: warp per row, no barrier.
 template <typename T, typename Emit>
 __device__ __forceinline__ void spmv_medium(const int *__restrict__ rp, const int *__restrict__ ci,
@@ -139,6 +169,10 @@ __device__ __forceinline__ void spmv_unit(const SpmvTile &t, const int *__restri
                                           T *s_val, T *red, Emit emit) {
     if (t.kind == 0) {
         spmv_short<T>(rp, ci, val, x, t.row0, t.row1, s_col, s_val, emit);
+    } else if (t.kind == 3) {
+        spmv_subwarp<T, 4>(rp, ci, val, x, t.row0, t.row1, emit);
+    } else if (t.kind == 4) {
+        spmv_subwarp<T, 8>(rp, ci, val, x, t.row0, t.row1, emit);
     } else if (t.kind == 1) {
         spmv_medium<T>(rp, ci, val, x, t.row0, t.row1, emit);
     } else {
