@@ -799,6 +799,27 @@ __global__ void k_sum_columns(const double *__restrict__ Y, int ld, int n, int k
 
 int map_status(int st) { return st == ST_CONVERGED ? HLANC_OK : HLANC_NOT_CONVERGED; }
 
+// Device -> host copy of `height` columns of `width` bytes, synchronous.  A
+// large pageable destination (the reference API's `new double[]`) is
+// page-locked for the copy, so it runs as one DMA instead of a staged
+// pageable copy (measured on GB300: 2 GB of Ritz vectors in 1.65 s staged).
+int copy_d2h_2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
+                cudaStream_t s) {
+    const size_t span = height ? dpitch * (height - 1) + width : 0;
+    bool registered = false;
+    if (span >= ((size_t)64 << 20)) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, dst) == cudaSuccess && a.type == cudaMemoryTypeUnregistered)
+            registered = cudaHostRegister(dst, span, cudaHostRegisterDefault) == cudaSuccess;
+        cudaGetLastError();   // an unregistrable range only means the staged copy
+    }
+    cudaError_t e = cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (registered) cudaHostUnregister(dst);
+    CK(e);
+    return HLANC_OK;
+}
+
 // Mixed precision: the FP32-SpMV phase stops at a relative tolerance of
 // 1e-6 (FP32 rounding of the SpMV sits near 1e-7) and gets a quarter of the
 // restart budget; the FP64 phase then has the whole budget.
@@ -891,8 +912,9 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
                 CK(cudaMemcpyAsync(values, p.small + SM_VALS(m), sizeof(double) * nconv, cudaMemcpyDeviceToDevice, E.stream));
             } else {
                 CK(cudaMemcpyAsync(values, p.small + SM_VALS(m), sizeof(double) * nconv, cudaMemcpyDeviceToHost, E.stream));
-                CK(cudaMemcpy2DAsync(vectors, sizeof(double) * (size_t)ldv, p.vout, sizeof(double) * (size_t)p.ldo,
-                                     sizeof(double) * (size_t)n, m, cudaMemcpyDeviceToHost, E.stream));
+                if ((rc = copy_d2h_2d(vectors, sizeof(double) * (size_t)ldv, p.vout, sizeof(double) * (size_t)p.ldo,
+                                      sizeof(double) * (size_t)n, m, E.stream)))
+                    return rc;
             }
             CK(cudaStreamSynchronize(E.stream));
         }
@@ -1563,9 +1585,10 @@ int srv_complete(Srv &s, Srv::Lane &L) {
         const int n = p.n, m = p.ncv;
         r.values.assign(p.values.begin(), p.values.begin() + p.hs.nconv);
         r.vectors.resize((size_t)n * m);
-        CK(cudaMemcpy2DAsync(r.vectors.data(), sizeof(double) * n, p.vout, sizeof(double) * p.ldo,
-                             sizeof(double) * n, m, cudaMemcpyDeviceToHost, E.stream));
-        CK(cudaStreamSynchronize(E.stream));
+        int rc;
+        if ((rc = copy_d2h_2d(r.vectors.data(), sizeof(double) * n, p.vout, sizeof(double) * p.ldo,
+                              sizeof(double) * n, m, E.stream)))
+            return rc;
         srv_finish(s, L, r, HLANC_OK);
     }
     L.ids.swap(keep);
