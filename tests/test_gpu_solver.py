@@ -125,6 +125,24 @@ def test_matches_oracle_on_same_start(H, oracle_mod):
     assert np.abs(vals[:6] - vals_o[:6]).max() <= EV_RTOL * np.abs(vals_o[:6]).max()
 
 
+@pytest.mark.parametrize("nev,ncv", [(1, 6), (2, 6), (2, 12)])
+def test_invariant_subspace_matches_oracle(H, oracle_mod, nev, ncv):
+    # two distinct eigenvalues: the Krylov space is exhausted after two steps,
+    # the third CGS pass fails and the residual is zeroed (HLanc.hpp:1452-1466);
+    # the reference and the oracle return 2.0 (multiplicity 100) nev times
+    n = 200
+    d = np.array([2.0 if i % 2 else -1.0 for i in range(n)])
+    m = G.CSR(n, n, np.arange(n + 1, dtype=np.int32), np.arange(n, dtype=np.int32), d)
+    x0 = G.start_vector(n, 3)
+    rc_o, vals_o, _, _ = oracle_mod.solve_csr(m.row_ptr, m.col, m.val, n, False, nev, ncv, x0)
+    op = H.dcsrmv_operator_gpu(m)
+    rc, vals, vecs, st = H.solve(op, nev, ncv, start=x0)
+    assert rc == rc_o == 0
+    assert np.abs(vals[:nev] - vals_o[:nev]).max() <= EV_RTOL * 2.0
+    R = d[:, None] * vecs[:, :nev] - vecs[:, :nev] * vals[:nev]
+    assert np.linalg.norm(R, axis=0).max() <= 1e-10 * 2.0
+
+
 def test_spmv_operator_host_and_device(H, readers_golden):
     import torch
     s = golden("spmv.npz")
