@@ -215,8 +215,9 @@ __device__ __forceinline__ void split8(const double (&x)[8], int emax, uint4 (&p
 // D_4 2^16 + D_5 2^8 + D_6 and S = ex + fx - 2106 (ex, fx: the biased
 // exponents the row and the column were split against).  Both halves are
 // placed exactly into doubles by adding them to the significand of
-// 1.5 * 2^(84+S) resp. 1.5 * 2^(52+S) (|hi|, |lo| < 2^51), so the value
-// costs three FP64 additions with one rounding.
+// A0 = 1.5 * 2^(84+S) resp. B0 = 1.5 * 2^(52+S) (|hi|, |lo| < 2^51).
+// A0 + B0 fits in 35 significant bits, so (A - (A0 + B0)) is exact and
+// the value costs two FP64 additions with one rounding.
 __device__ __forceinline__ double combine(const float (&d)[NDIG], int ex, int fx) {
     // every level is an integer below 2^26 in magnitude
     const long long l0 = __float2int_rn(d[0]), l1 = __float2int_rn(d[1]), l2 = __float2int_rn(d[2]);
@@ -230,9 +231,9 @@ __device__ __forceinline__ double combine(const float (&d)[NDIG], int ex, int fx
         const long long half = 1LL << 51;                             // 1.5 = 1 + 2^-1
         const double A = __longlong_as_double((eA << 52) + half + hi);
         const double B = __longlong_as_double((eB << 52) + half + lo);
-        const double cA = __longlong_as_double((eA << 52) + half);
-        const double cB = __longlong_as_double((eB << 52) + half);
-        return (A - cA) + (B - cB);
+        // A0 + B0: B0 is 1.5 * 2^20 units of A0's last place (2^(32+S))
+        const double cAB = __longlong_as_double((eA << 52) + half + (3LL << 19));
+        return (A - cAB) + B;
     }
     return scalbn(fma((double)hi, 4294967296.0, (double)lo), S);
 }
@@ -255,12 +256,11 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
 
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *sA = smem;                                   // NDIG x BM x kpad bf16
-    // Q's digit planes stacked: rows (t + 6) * NPAD + i hold plane t of output
-    // i (t = 0..6); the six blocks before them are zero.  The B operand of A
-    // plane s is this stack shifted by (6 - s) blocks, so one MMA over
-    // N = 7 * NPAD columns adds plane s's share to every level L at once
-    // (block L of the window is plane L - s, or zero).
-    unsigned char *sB = smem + (size_t)NDIG * BM * KMAX * 2;    // 13 x NPAD x kpad bf16
+    // Q's digit planes stacked: rows t * NPAD + i hold plane t of output i
+    // (t = 0..6).  Plane s of V contributes to levels L = s..6 only, so its
+    // MMA writes accumulator columns [s * NPAD, 7 * NPAD) with the stack's
+    // first (7 - s) * NPAD rows as B: column block L meets plane L - s.
+    unsigned char *sB = smem + (size_t)NDIG * BM * KMAX * 2;    // 7 x NPAD x kpad bf16
     __shared__ uint64_t s_mbar;
     __shared__ uint32_t s_taddr;
     __shared__ int s_rowexp[2][BM];
@@ -272,8 +272,6 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
     const double *Q = P.small + SM_Q(m);
     const double *h = P.small + SM_H(m);
     const size_t aplane = (size_t)BM * kpad * 2, bplane = (size_t)NPAD * kpad * 2;
-    for (int i = tid; i < (int)(6 * bplane / 16); i += THREADS)
-        reinterpret_cast<uint4 *>(sB)[i] = make_uint4(0u, 0u, 0u, 0u);
 
     prefetch_rows_l2(P.V, (size_t)P.ld, m, t.row0, min(BM, t.row1 - t.row0));
     if (warp == 0) {
@@ -311,14 +309,10 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
         split8(x, s_colexp[i], pl);
         const uint32_t off = kmajor_off(i, 8 * g, kpad);
 #pragma unroll
-        for (int s = 0; s < NDIG; ++s) *reinterpret_cast<uint4 *>(sB + (s + 6) * bplane + off) = pl[s];
+        for (int s = 0; s < NDIG; ++s) *reinterpret_cast<uint4 *>(sB + s * bplane + off) = pl[s];
     }
 
-    // N = 7 * NPAD in one MMA, or two (each N <= 256, a multiple of 16)
-    constexpr int NTOT = NDIG * NPAD;
-    constexpr int N1 = NTOT <= 256 ? NTOT : ((NTOT / 2 + 15) / 16) * 16;
-    constexpr int N2 = NTOT - N1;
-    const uint32_t idesc1 = instr_desc(BM, N1), idesc2 = instr_desc(BM, N2 > 0 ? N2 : 16);
+
     const uint32_t sbo = (uint32_t)kg * 128u;
     const uint32_t taddr = s_taddr;
     const double hn = h[nev];
@@ -371,15 +365,18 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
         if (tid == 0) {
             fence_after();
             const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-            const uint32_t n1_bytes = (uint32_t)(N1 / 8) * sbo;     // N1 rows further in the stack
             for (int s = 0; s < NDIG; ++s) {
-                const uint32_t bs = b0 + (uint32_t)((6 - s) * bplane);
+                // N = (7 - s) * NPAD columns, in one MMA or two (each <= 256, a multiple of 16)
+                const int ns = (NDIG - s) * NPAD;
+                const int n1 = ns <= 256 ? ns : ((ns / 2 + 15) / 16) * 16, n2 = ns - n1;
+                const uint32_t id1 = instr_desc(BM, n1), id2 = instr_desc(BM, n2 > 0 ? n2 : 16);
+                const uint32_t d0 = taddr + (uint32_t)(s * NPAD);
+                const uint32_t n1_bytes = (uint32_t)(n1 / 8) * sbo;   // n1 rows further in the stack
                 for (int kk = 0; kk < kpad / 16; ++kk) {
                     const uint64_t ad = smem_desc(a0 + (uint32_t)(s * aplane) + kk * 256u, 128u, sbo);
                     const uint32_t acc = (s | kk) ? 1u : 0u;
-                    mma(taddr, ad, smem_desc(bs + kk * 256u, 128u, sbo), idesc1, acc);
-                    if (N2 > 0)
-                        mma(taddr + (uint32_t)N1, ad, smem_desc(bs + n1_bytes + kk * 256u, 128u, sbo), idesc2, acc);
+                    mma(d0, ad, smem_desc(b0 + kk * 256u, 128u, sbo), id1, acc);
+                    if (n2 > 0) mma(d0 + (uint32_t)n1, ad, smem_desc(b0 + n1_bytes + kk * 256u, 128u, sbo), id2, acc);
                 }
             }
             mma_commit(&s_mbar);
@@ -458,7 +455,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
 
 template <int NPAD>
 static size_t basis_tc_smem() {
-    return (size_t)tc::NDIG * tc::BM * tc::KMAX * 2 + (size_t)13 * NPAD * tc::KMAX * 2;
+    return (size_t)tc::NDIG * tc::BM * tc::KMAX * 2 + (size_t)tc::NDIG * NPAD * tc::KMAX * 2;
 }
 
 template <int NPAD>
