@@ -961,7 +961,7 @@ int hlanc_version(int *major, int *minor) {
     return HLANC_OK;
 }
 
-long long hlanc_kernel_launches(void) { return launch_counter(); }
+long long hlanc_kernel_launches(void) { return launch_counter().load(); }
 
 void hlanc_opts_default(hlanc_opts_t *o) {
     memset(o, 0, sizeof(*o));

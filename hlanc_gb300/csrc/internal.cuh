@@ -14,6 +14,7 @@
 // order.  A batch is simply several problems whose tiles share one launch.
 #pragma once
 
+#include <atomic>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -266,7 +267,8 @@ void launch_residuals(const int *row_ptr, const int *col, const double *val, int
                       const double *values_d, const double *vectors_d, int ldv, double *out4k,
                       cudaStream_t s);
 
-long long &launch_counter();
+// Kernels this library launched (all host threads).
+std::atomic<long long> &launch_counter();
 
 // Read-only view of a device CSR operator's arrays (engine.cu).
 struct CsrView {

@@ -21,8 +21,8 @@
 
 namespace hlanc {
 
-long long &launch_counter() {
-    static long long c = 0;
+std::atomic<long long> &launch_counter() {
+    static std::atomic<long long> c{0};
     return c;
 }
 
