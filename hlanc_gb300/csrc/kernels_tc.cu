@@ -21,13 +21,23 @@
 //    lower levels can round by a few units at weights 2^-32 .. 2^-48 of
 //    level 0, i.e. below FP64 precision.  Levels past 6 are dropped
 //    (weight <= 2^-56 of the result's scale).
-//  * the levels are recombined per output in 64-bit integers and two
-//    FP64 conversions: 4 FP64 instructions per output instead of ~50 FMAs.
+//  * the levels are recombined per output in 64-bit integers, placed
+//    exactly into two doubles through their bit patterns, and added: two
+//    FP64 instructions per output instead of ~50 FMAs.
+//  * plane s of V only feeds levels s..6, so each plane's MMA covers N =
+//    (7 - s) * NPAD accumulator columns.
 //
-// Shapes: M = 128 rows per MMA, N = padded nev + 1 (<= 64), K = ncv padded
-// to 16 (<= 64).  Operands live in shared memory in the no-swizzle K-major
-// layout (8-row x 16-byte core matrices); the accumulators (7 x N columns)
-// in tensor memory.  One CTA per tile of rows, one CTA per SM.
+// Shapes: M = 128 rows per MMA, NPAD = nev + 1 padded to 16 (<= 64), K =
+// ncv padded to 16 (<= 64).  Operands live in shared memory in the
+// no-swizzle K-major layout (8-row x 16-byte core matrices); the
+// accumulators (7 x NPAD columns) in tensor memory.  One CTA per tile of
+// rows, one CTA per SM.  Measured on GB300 at n = 4.1M, ncv = 60: 2.7 ms
+// (nev 20) and 3.8 ms (nev 40) against 8.8 / 17.8 ms for the FP64 kernel.
+//
+// The same splitting was tried for the CGS passes (w -= V h, h = V^T w),
+// where each element of V meets a single output: the splitting alone costs
+// more issue slots per element than the FP64 kernels' DFMA, so those stay
+// on the FP64 pipe.
 #include <cuda_bf16.h>
 
 #include "internal.cuh"
