@@ -135,6 +135,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def cgs_fp64_share(kind: str, nev: int, ncv: int) -> float:
+    """Fraction of a CGS kernel's columns run as FP64 FMAs by the hybrid
+    kernels (kernels_step.cu), over the column counts c = nev+1 .. ncv of one
+    restart cycle: projection panels of 8 split 5 + 3 (tails 1,1,2,2,3,3,4 of
+    1..7), the update runs whole groups of 8 (about c/2) in FP64."""
+    tail = [0, 1, 1, 2, 2, 3, 3, 4]
+    f = t = 0
+    for c in range(nev + 1, ncv + 1):
+        if kind == "cgs_proj":
+            f += 5 * (c // 8) + tail[c % 8]
+        else:
+            f += c if c < 8 else ((c + 8) >> 4) << 3
+        t += c
+    return f / t
+
+
 def read_traffic_ratio(kernel_class: str):
     """DRAM bytes / algorithmic bytes of a kernel class from the committed ncu
     summary (profiles/*.txt line 'traffic_ratio_dram_over_algorithmic <class> <r>');
@@ -568,15 +584,23 @@ def main():
     achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9 if d["ms"] else 0.0
     ratio = read_traffic_ratio(dom)
     traffic = ratio * d["bytes"] / max(d["launches"], 1) if ratio else None
+    # share of the dominant kernel's multiply-adds issued as FP64 FMAs: the
+    # hybrid CGS kernels run 5 of every 8 projection columns and about half
+    # of the update columns in FP64, the rest as exact integer products
+    hybrid = m.n >= H.CGS_HYBRID_MIN_ROWS and dom in ("cgs_proj", "cgs_apply")
+    fp64_share = cgs_fp64_share(dom, nev, ncv) if hybrid else 1.0
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "traffic": traffic, "traffic_source": "ncu dram bytes / algorithmic bytes (profiles/) x "
                                                           "algorithmic bytes per launch" if ratio else None,
                 "bytes_per_launch": d["bytes"] / max(d["launches"], 1),
                 "avg_launch_ms": d["ms"] / max(d["launches"], 1),
-                "fp64": {"achieved_tflops": d["flops"] / (d["ms"] * 1e-3) / 1e12 if d["ms"] else 0.0,
-                         "peak_tflops": fp64_peak, "frac": (d["flops"] / (d["ms"] * 1e-3) / 1e12) / fp64_peak
-                         if d["ms"] else 0.0, "peak_source": "measured live (hlanc_diag_fp64_tflops)"},
+                "cgs_kernels": "hybrid FP64 + exact integer" if hybrid else "fp64",
+                "fp64": {"achieved_tflops": fp64_share * d["flops"] / (d["ms"] * 1e-3) / 1e12 if d["ms"] else 0.0,
+                         "peak_tflops": fp64_peak,
+                         "frac": (fp64_share * d["flops"] / (d["ms"] * 1e-3) / 1e12) / fp64_peak if d["ms"] else 0.0,
+                         "fp64_share_of_flops": fp64_share,
+                         "peak_source": "measured live (hlanc_diag_fp64_tflops)"},
                 "time_share": {k: prof[k]["ms"] / total_kernel_ms for k in kernel_classes + ["aux"]},
                 "host_restart_ms": prof["host_restart"]["ms"]}
     line = {"metric": "converged eigenpairs/s (resid <= 1e-10 ||A||)", "value": value, "unit": "eigenpairs/s",

@@ -28,6 +28,10 @@ HLANC_PREC_FP64 = 0
 HLANC_PREC_FP32_REFINE = 1
 HLANC_BASIS_AUTO = 0
 HLANC_BASIS_FP64 = 1
+HLANC_CGS_AUTO = 0
+HLANC_CGS_FP64 = 1
+HLANC_CGS_HYBRID = 2
+CGS_HYBRID_MIN_ROWS = 1 << 18     # HLANC_CGS_AUTO picks the hybrid kernels from this many rows
 HLANC_MAX_NCV = 128
 HLANC_MAX_NEV = 63
 
@@ -45,7 +49,7 @@ class Opts(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_restarts", C.c_int), ("precision", C.c_int),
                 ("seed", C.c_ulonglong), ("start", C.POINTER(C.c_double)), ("stream", C.c_void_p),
                 ("use_graphs", C.c_int), ("restart_on_device", C.c_int), ("profile", C.c_int),
-                ("basis_kernel", C.c_int), ("reserved", C.c_int * 4)]
+                ("basis_kernel", C.c_int), ("cgs_kernel", C.c_int), ("reserved", C.c_int * 3)]
 
 
 class Stats(C.Structure):
@@ -155,10 +159,12 @@ def _check(rc: int, what: str) -> None:
 
 def opts(tol: float = 0.0, max_restarts: int = 200, precision: int = HLANC_PREC_FP64, seed: int = 0,
          start: Optional[np.ndarray] = None, stream: int = 0, use_graphs: bool = True,
-         restart_on_device: bool = False, profile: bool = False, basis_fp64: bool = False):
+         restart_on_device: bool = False, profile: bool = False, basis_fp64: bool = False,
+         cgs: int = HLANC_CGS_AUTO):
     o = Opts()
     lib().hlanc_opts_default(C.byref(o))
     o.basis_kernel = HLANC_BASIS_FP64 if basis_fp64 else HLANC_BASIS_AUTO
+    o.cgs_kernel = cgs
     o.tol, o.max_restarts, o.precision, o.seed = tol, max_restarts, precision, seed
     o.use_graphs = int(use_graphs)
     o.restart_on_device = int(restart_on_device)

@@ -306,6 +306,8 @@ public:
     cudaMemPool_t pool = nullptr;        // when set, problems allocate from it on `stream`
     int min_tile_rows = 128;
     bool basis_tc = true;                // basis update on the tensor cores when the shape fits
+    int cgs_mode = HLANC_CGS_AUTO;       // CGS panels split between the FP64 and the integer pipes
+    long long rows_active = 0;           // rows of all problems in the launch tables
     std::vector<ProbRes> probs;
     std::vector<int> active;             // problems in the launch tables, in slot order
     Problem *P_d = nullptr;
@@ -379,6 +381,16 @@ public:
         return HLANC_OK;
     }
 
+    // The hybrid CGS kernels pay a little latency per launch (the scale scan
+    // of w, per-row conversions) for throughput; launches over few rows are
+    // latency-bound and keep the FP64 kernels (measured on GB300: the
+    // 10,000-row Laplacian solve took 100.6 ms hybrid against 90.1 ms FP64;
+    // the 4.1M-row solve 4.95 s against 5.41 s).
+    static constexpr long long CGS_HYBRID_MIN_ROWS = 1 << 18;
+    bool hybrid_cgs() const {
+        return cgs_mode == HLANC_CGS_HYBRID || (cgs_mode == HLANC_CGS_AUTO && rows_active >= CGS_HYBRID_MIN_ROWS);
+    }
+
     // Rebuild the descriptor/tile tables and the mailbox layout for `active`.
     int upload() {
         std::vector<Problem> P(active.size());
@@ -386,6 +398,7 @@ public:
         std::vector<SpmvTile> ST;
         max_ncv = 0;
         fp32_any = false;
+        rows_active = 0;
         off_h.assign(active.size(), 0);
         long long off = 0;
         for (size_t a = 0; a < active.size(); ++a) {
@@ -419,6 +432,7 @@ public:
                 }
             max_ncv = std::max(max_ncv, p.ncv);
             fp32_any = fp32_any || p.fp32;
+            rows_active += p.n;
             off_h[a] = off;
             off += mbox_slot(p.ncv);
         }
@@ -500,7 +514,7 @@ public:
         const int na = (int)active.size();
         if (!device_restart) launch_scatter(P_d, na, off_d, flag_d, mbox_d, stream);
         if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), basis_tc, stream);
-        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, stream);
+        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, hybrid_cgs(), stream);
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
     }
@@ -595,7 +609,7 @@ public:
             if (p.host_op(p.host_ctx, xs_h, ys_h) != 0) return HLANC_ERR_CALLBACK;
             double *w = ((j + 1) & 1) ? p.r1 : p.r0;
             CK(cudaMemcpyAsync(w, ys_h, sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
-            launch_step(P_d, T_d, ntiles, S_d, nstiles, s, false, true, stream);
+            launch_step(P_d, T_d, ntiles, S_d, nstiles, s, false, true, hybrid_cgs(), stream);
         }
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
@@ -860,6 +874,7 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
     int rc = E.init(dev, o.stream, o.use_graphs != 0, o.restart_on_device != 0);
     if (rc) return rc;
     E.basis_tc = o.basis_kernel != HLANC_BASIS_FP64;
+    E.cgs_mode = o.cgs_kernel;
     const bool fp32 = csr && o.precision == HLANC_PREC_FP32_REFINE && csr->val32_d;
     int idx = 0;
     const hlanc_opts_t o1 = fp32 ? fp32_phase_opts(o) : o;
@@ -975,6 +990,7 @@ void hlanc_opts_default(hlanc_opts_t *o) {
     o->restart_on_device = 0;
     o->profile = 0;
     o->basis_kernel = HLANC_BASIS_AUTO;
+    o->cgs_kernel = HLANC_CGS_AUTO;
 }
 
 int hlanc_last_profile(hlanc_profile_t *out) {
@@ -1360,6 +1376,7 @@ int hlanc_batch_create(int dev, int nprob, const hlanc_csr_t *ops, const int *ne
     int rc = b->E.init(dev, b->o.stream, b->o.use_graphs != 0, b->o.restart_on_device != 0);
     if (rc) return rc;
     b->E.basis_tc = b->o.basis_kernel != HLANC_BASIS_FP64;
+    b->E.cgs_mode = b->o.cgs_kernel;
     if (nprob > 1) b->E.min_tile_rows = BATCH_MIN_TILE_ROWS;
     const bool fp32 = b->o.precision == HLANC_PREC_FP32_REFINE;
     const hlanc_opts_t o1 = fp32 ? fp32_phase_opts(b->o) : b->o;
@@ -1734,7 +1751,7 @@ int srv_launch(Srv &s, Srv::Lane &L) {
     if (basis_nev > 0)
         launch_basis(E.P_d, E.T_d, E.ntiles, E.max_ncv, Engine::basis_bucket(basis_nev), E.basis_tc, E.stream);
     for (int k = 0; k < steps; ++k)
-        launch_step(E.P_d, E.T_d, E.ntiles, E.S_d, E.nstiles, k, E.fp32_any, false, E.stream);
+        launch_step(E.P_d, E.T_d, E.ntiles, E.S_d, E.nstiles, k, E.fp32_any, false, E.hybrid_cgs(), E.stream);
     launch_gather(E.P_d, na, E.off_d, E.mbox_d, E.stream);
     if ((rc = E.pull_async())) return rc;
     CK(cudaEventRecord(L.ev1, E.stream));

@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include "../../include/hlanc_gb300.h"
+#include "fixed_point.cuh"
 
 namespace hlanc {
 
@@ -243,7 +244,7 @@ void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, in
                          unsigned long long seed, cudaStream_t s);
 void launch_norm_init(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s);
 void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const SpmvTile *stiles_d,
-                 int nstiles, int step, bool fp32_any, bool external_w, cudaStream_t s);
+                 int nstiles, int step, bool fp32_any, bool external_w, bool cgs_hybrid, cudaStream_t s);
 void launch_prep_f32(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, cudaStream_t s);
 void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, double *xout,
                      cudaStream_t s);

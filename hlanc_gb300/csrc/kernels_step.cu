@@ -230,57 +230,119 @@ __global__ void __launch_bounds__(TPB) k_prep(const Problem *__restrict__ probs,
 }
 
 // ---- CGS projection: h = V[:, 0:c)^T w  (+ ||w||^2 on pass 1) ----------------
-// Thread per row, columns in panels of at most 16: each thread keeps one
-// accumulator per panel column for all the rows it visits in the tile (one
-// FP64 FMA per loaded element, coalesced column reads), then one transposed
-// warp reduction per 8 columns and a cross-warp sum in shared memory.  The
-// panel width is a template parameter picked from the device-known column
-// count, so no FP64 instruction is issued for an absent column
-// (predicated-off FP64 instructions still occupy GB300's FP64 pipe).  Measured
-// on GB300 against warp-per-column layouts and 8/24/32-column panels, 16
-// columns (64 registers, 4 CTAs per SM) was fastest.
-// Panel of NC (<= 16) consecutive columns starting at c0.
-template <int NC>
-__device__ __forceinline__ void proj_rows(const Problem &P, const Tile &t, const double *__restrict__ w, int c0,
-                                          bool with_norm, double *red, double *sm) {
+// Thread per row, columns in panels of at most 8: each thread keeps one
+// accumulator per panel column for all the rows it visits in the tile
+// (coalesced column reads), then one transposed warp reduction and a
+// cross-warp sum in shared memory.  Panel shapes are template parameters
+// picked from the device-known column count, so no instruction is issued
+// for an absent column (predicated-off FP64 instructions still occupy
+// GB300's FP64 pipe).
+//
+// The hybrid kernel (HY) splits a full panel into 5 FP64 columns (one DFMA
+// per element) and 3 integer columns (exact fixed-point products, fx_*),
+// which keeps the FP64 and the integer pipes busy at once.  Measured on
+// GB300 (n = 4.1M rows, 32 columns, HBM-resident V): 176 us against 254 us
+// for all-FP64 panels (8- or 16-wide), i.e. 5.9 against 4.1 TB/s; 4+4 was
+// equal, 3+5, 2+6 and 6+6 splits and 3, 5 or 6 CTAs per SM were slower.
+// w's fixed-point scale is the largest exponent of the thread's own rows on
+// pass 1 (one extra read of w, which also gives ||w||^2) and 2 ||w|| on
+// later passes (||w|| is known from the previous k_apply).
+template <int ND, int NI>
+__device__ __forceinline__ void proj_panel(const double *__restrict__ V, size_t ld, int row0, int row1,
+                                           const double *__restrict__ w, int c0, int ew, bool with_norm,
+                                           double *red, double *sm) {
+    constexpr int NC = ND + NI;
+    static_assert(NC >= 1 && NC <= 8, "panel width");
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t ld = (size_t)P.ld;
-    constexpr int NA = (NC + 7) / 8 * 8;
-    double acc[NA];
+    double acc[8];
 #pragma unroll
-    for (int i = 0; i < NA; ++i) acc[i] = 0.0;
+    for (int i = 0; i < 8; ++i) acc[i] = 0.0;
+    FxAcc A[NI > 0 ? NI : 1];
+#pragma unroll
+    for (int i = 0; i < NI; ++i) fx_zero(A[i]);
+    const int rsw = 1027 + ew;
     double nrm = 0.0;
-    for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
+    int steps = 0;
+    const double *__restrict__ vc = V + (size_t)c0 * ld;
+    for (int r = row0 + (int)threadIdx.x; r < row1; r += TPB) {
         const double wr = w[r];
         if (with_norm) nrm = fma(wr, wr, nrm);
-        const double *__restrict__ vr = P.V + r + (size_t)c0 * ld;
+        const double *__restrict__ vr = vc + r;
 #pragma unroll
-        for (int k = 0; k < NC; ++k) acc[k] = fma(__ldcs(vr + (size_t)k * ld), wr, acc[k]);
+        for (int k = 0; k < ND; ++k) acc[k] = fma(__ldcs(vr + (size_t)k * ld), wr, acc[k]);
+        if constexpr (NI > 0) {
+            int w1, w0;
+            fx_split(wr, rsw, w1, w0);
+#pragma unroll
+            for (int k = 0; k < NI; ++k) {
+                int v1, v0;
+                fx_split(__ldcs(vr + (size_t)(ND + k) * ld), FX_RS_UNIT, v1, v0);
+                fx_mac(A[k], v1, v0, w1, w0);
+            }
+            if (++steps == FX_MACS) {
+                steps = 0;
+#pragma unroll
+                for (int k = 0; k < NI; ++k) fx_carry(A[k]);
+            }
+        }
     }
-    // lane l holds, per group g of 8 columns, the warp sum of column 8g + (l >> 2)
+    // products carry the scales 2^57 (V) and 2^(57 - ew) (w)
 #pragma unroll
-    for (int g = 0; g < NA / 8; ++g) {
-        const double v = warp_reduce8(acc + 8 * g);
-        if ((lane & 3) == 0) sm[warp * 32 + 8 * g + (lane >> 2)] = v;
+    for (int k = 0; k < NI; ++k) acc[ND + k] = fx_to_double(A[k], ew - 114);
+    // lane l holds the warp sum of column l >> 2
+    {
+        const double v = warp_reduce8(acc);
+        if ((lane & 3) == 0) sm[warp * 8 + (lane >> 2)] = v;
     }
     if (with_norm) {
         nrm = warp_sum(nrm);
-        if (lane == 0) sm[8 * 32 + warp] = nrm;
+        if (lane == 0) sm[8 * 8 + warp] = nrm;
     }
     __syncthreads();
     if (threadIdx.x < NC) {
         double s = 0.0;
-        for (int q = 0; q < TPB / 32; ++q) s += sm[q * 32 + threadIdx.x];
+        for (int q = 0; q < TPB / 32; ++q) s += sm[q * 8 + threadIdx.x];
         red[c0 + threadIdx.x] = s;
     }
     if (with_norm && threadIdx.x == 32) {
         double s = 0.0;
-        for (int q = 0; q < TPB / 32; ++q) s += sm[8 * 32 + q];
+        for (int q = 0; q < TPB / 32; ++q) s += sm[8 * 8 + q];
         red[c0 + NC] = s;
     }
     __syncthreads();
 }
 
+__device__ __forceinline__ void proj_panel_fp64(const double *__restrict__ V, size_t ld, int row0, int row1,
+                                                const double *__restrict__ w, int c0, int cc, bool nrm,
+                                                double *red, double *sm) {
+    switch (cc) {
+    case 1: proj_panel<1, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
+    case 2: proj_panel<2, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
+    case 3: proj_panel<3, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
+    case 4: proj_panel<4, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
+    case 5: proj_panel<5, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
+    case 6: proj_panel<6, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
+    case 7: proj_panel<7, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
+    default: proj_panel<8, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
+    }
+}
+
+__device__ __forceinline__ void proj_panel_hybrid(const double *__restrict__ V, size_t ld, int row0, int row1,
+                                                  const double *__restrict__ w, int c0, int cc, int ew,
+                                                  double *red, double *sm) {
+    switch (cc) {
+    case 1: proj_panel<1, 0>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
+    case 2: proj_panel<1, 1>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
+    case 3: proj_panel<2, 1>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
+    case 4: proj_panel<2, 2>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
+    case 5: proj_panel<3, 2>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
+    case 6: proj_panel<3, 3>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
+    case 7: proj_panel<4, 3>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
+    default: proj_panel<5, 3>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
+    }
+}
+
+template <bool HY>
 __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ probs,
                                               const Tile *__restrict__ tiles, int s, int pass) {
     const Tile t = tiles[blockIdx.x];
@@ -292,29 +354,34 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
     const int c = j + 1;
     const int m = P.ncv;
     const double *__restrict__ w = step_out(P, j);
+    const double *__restrict__ V = P.V;
+    const size_t ld = (size_t)P.ld;
     __shared__ double red[MAXNCV + 1], tot[MAXNCV + 1];
-    __shared__ double sm[9 * 32];
-    for (int c0 = 0; c0 < c; c0 += 16) {
-        const int cc = min(16, c - c0);
-        const bool nrm = pass == 1 && c0 + cc == c;
-        switch (cc) {
-        case 1: proj_rows<1>(P, t, w, c0, nrm, red, sm); break;
-        case 2: proj_rows<2>(P, t, w, c0, nrm, red, sm); break;
-        case 3: proj_rows<3>(P, t, w, c0, nrm, red, sm); break;
-        case 4: proj_rows<4>(P, t, w, c0, nrm, red, sm); break;
-        case 5: proj_rows<5>(P, t, w, c0, nrm, red, sm); break;
-        case 6: proj_rows<6>(P, t, w, c0, nrm, red, sm); break;
-        case 7: proj_rows<7>(P, t, w, c0, nrm, red, sm); break;
-        case 8: proj_rows<8>(P, t, w, c0, nrm, red, sm); break;
-        case 9: proj_rows<9>(P, t, w, c0, nrm, red, sm); break;
-        case 10: proj_rows<10>(P, t, w, c0, nrm, red, sm); break;
-        case 11: proj_rows<11>(P, t, w, c0, nrm, red, sm); break;
-        case 12: proj_rows<12>(P, t, w, c0, nrm, red, sm); break;
-        case 13: proj_rows<13>(P, t, w, c0, nrm, red, sm); break;
-        case 14: proj_rows<14>(P, t, w, c0, nrm, red, sm); break;
-        case 15: proj_rows<15>(P, t, w, c0, nrm, red, sm); break;
-        case 16: proj_rows<16>(P, t, w, c0, nrm, red, sm); break;
-        default: break;
+    __shared__ double sm[9 * 8 + 32];
+    if constexpr (HY) {
+        int ew;
+        if (pass == 1) {
+            // ||w||^2 and the scale of this thread's rows (HLanc.hpp:1429)
+            unsigned mx = 0;
+            double nrm = 0.0;
+            for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
+                const double x = w[r];
+                nrm = fma(x, x, nrm);
+                mx = max(mx, fx_hi_abs(x));
+            }
+            ew = fx_scale(mx);
+            nrm = block_sum0(nrm, sm);
+            if (threadIdx.x == 0) red[c] = nrm;
+            __syncthreads();
+        } else {
+            ew = fx_scale(fx_hi_abs(S->rnorm)) + 1;   // |w_i| <= ||w|| < 2^(ew + 1)
+        }
+        for (int c0 = 0; c0 < c; c0 += 8)
+            proj_panel_hybrid(V, ld, t.row0, t.row1, w, c0, min(8, c - c0), ew, red, sm);
+    } else {
+        for (int c0 = 0; c0 < c; c0 += 8) {
+            const int cc = min(8, c - c0);
+            proj_panel_fp64(V, ld, t.row0, t.row1, w, c0, cc, pass == 1 && c0 + cc == c, red, sm);
         }
     }
     __syncthreads();
@@ -336,7 +403,14 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
 }
 
 // ---- CGS update: w -= V[:, 0:c) h ; DGKS decision ------------------------------
-__global__ void __launch_bounds__(TPB, 6) k_apply(const Problem *__restrict__ probs,
+// The hybrid kernel (HY) runs about half of the columns (whole groups of 8)
+// as FP64 FMAs and the rest as exact fixed-point products (h scaled by its
+// largest entry); the integer sum of a row is converted once and subtracted.
+// Measured on GB300 (n = 4.1M, 32 columns): 186 us against 245 us for the
+// all-FP64 loop; interleaving 4 + 4 columns inside every group of 8 was no
+// faster than all-FP64 in the solver.
+template <bool HY>
+__global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__restrict__ probs,
                                                const Tile *__restrict__ tiles, int s, int pass) {
     const Tile t = tiles[blockIdx.x];
     const Problem &P = probs[t.prob];
@@ -348,25 +422,78 @@ __global__ void __launch_bounds__(TPB, 6) k_apply(const Problem *__restrict__ pr
     const int m = P.ncv;
     double *__restrict__ w = step_out(P, j);
     __shared__ double hs[MAXNCV];
+    __shared__ int h1s[MAXNCV], h0s[MAXNCV];
     __shared__ double scratch[32], mine[1], tot[1];
     __shared__ int s_zero;
+    __shared__ unsigned s_hmax;
     const double *hv = P.small + SM_HV(m);
-    for (int i = threadIdx.x; i < c; i += TPB) hs[i] = hv[i];
+    if (threadIdx.x == 0) s_hmax = 0u;
+    __syncthreads();
+    for (int i = threadIdx.x; i < c; i += TPB) {
+        hs[i] = hv[i];
+        if (HY) atomicMax(&s_hmax, fx_hi_abs(hv[i]));
+    }
+    __syncthreads();
+    const int eh = fx_scale(s_hmax);
+    if (HY)
+        for (int i = threadIdx.x; i < c; i += TPB) fx_split(hs[i], 1027 + eh, h1s[i], h0s[i]);
     __syncthreads();
     const size_t ld = (size_t)P.ld;
+    // FP64 share: whole groups of 8, about half of the columns (all below 8)
+    const int cd = c < 8 ? c : ((c + 8) >> 4) << 3;
     double nrm = 0.0;
     for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
         const double *__restrict__ vr = P.V + r;
         double acc = w[r];
         int k = 0;
-        for (; k + 8 <= c; k += 8) {
-            double v[8];
+        if constexpr (HY) {
+            // columns [0, cd) as FP64 FMAs, [cd, c) as exact integer products
+            for (; k + 8 <= cd; k += 8) {
+                double v[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
+                for (int q = 0; q < 8; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
 #pragma unroll
-            for (int q = 0; q < 8; ++q) acc = fma(-v[q], hs[k + q], acc);
+                for (int q = 0; q < 8; ++q) acc = fma(-v[q], hs[k + q], acc);
+            }
+            for (; k < cd; ++k) acc = fma(-__ldcs(vr + (size_t)k * ld), hs[k], acc);
+            if (k < c) {
+                FxAcc A;
+                fx_zero(A);
+                int steps = 0;
+                for (; k + 8 <= c; k += 8) {
+                    double v[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        int x1, x0;
+                        fx_split(v[q], FX_RS_UNIT, x1, x0);
+                        fx_mac(A, x1, x0, h1s[k + q], h0s[k + q]);
+                    }
+                    steps += 8;
+                    if (steps == FX_MACS) {
+                        steps = 0;
+                        fx_carry(A);
+                    }
+                }
+                // at most 7 more steps after 0 or 8: within the carry budget
+                for (; k < c; ++k) {
+                    int x1, x0;
+                    fx_split(__ldcs(vr + (size_t)k * ld), FX_RS_UNIT, x1, x0);
+                    fx_mac(A, x1, x0, h1s[k], h0s[k]);
+                }
+                acc -= fx_to_double(A, eh - 114);
+            }
+        } else {
+            for (; k + 8 <= c; k += 8) {
+                double v[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) acc = fma(-v[q], hs[k + q], acc);
+            }
+            for (; k < c; ++k) acc = fma(-__ldcs(vr + (size_t)k * ld), hs[k], acc);
         }
-        for (; k < c; ++k) acc = fma(-__ldcs(vr + (size_t)k * ld), hs[k], acc);
         w[r] = acc;
         nrm = fma(acc, acc, nrm);
     }
@@ -503,7 +630,7 @@ void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int st
 // One Lanczos step for every active problem of the tile table.  With
 // external_w the operator output was already written by the host path.
 void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const SpmvTile *stiles_d,
-                 int nstiles, int step, bool fp32_any, bool external_w, cudaStream_t s) {
+                 int nstiles, int step, bool fp32_any, bool external_w, bool cgs_hybrid, cudaStream_t s) {
     if (!external_w) {
         if (fp32_any) {
             prof_begin(s);
@@ -521,10 +648,12 @@ void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const Spmv
     }
     for (int pass = 1; pass <= 3; ++pass) {
         prof_begin(s);
-        k_proj<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+        if (cgs_hybrid) k_proj<true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+        else k_proj<false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
         prof_end(KC_PROJ, s);
         prof_begin(s);
-        k_apply<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+        if (cgs_hybrid) k_apply<true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+        else k_apply<false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
         prof_end(KC_APPLY, s);
     }
     launch_counter() += 6;

@@ -42,6 +42,15 @@ extern "C" {
                                         ncv <= 64 and nev <= 60, else the FP64 kernel */
 #define HLANC_BASIS_FP64          1  /* always the FP64 CUDA-core kernel */
 
+/* Arithmetic of the CGS passes h = V^T w, w -= V h (hlanc_opts_t.cgs_kernel).
+ * The hybrid kernels run about half of every column panel as FP64 FMAs and
+ * the rest as exact fixed-point integer products (inputs quantised to 2^-58
+ * of their scale, sums exact), so the FP64 and the integer pipes work at
+ * the same time. */
+#define HLANC_CGS_AUTO            0  /* hybrid for launches over >= 2^18 rows, else FP64 */
+#define HLANC_CGS_FP64            1  /* every column as FP64 FMAs */
+#define HLANC_CGS_HYBRID          2  /* hybrid at every size */
+
 /* Largest ncv the device restart kernels accept, and largest nev. */
 #define HLANC_MAX_NCV           128
 #define HLANC_MAX_NEV            63
@@ -107,7 +116,8 @@ typedef struct {
     int restart_on_device;    /* run the O(ncv^2) restart math in a device kernel instead of on the host */
     int profile;              /* time every kernel launch with CUDA events (eager launches); see hlanc_last_profile */
     int basis_kernel;         /* HLANC_BASIS_*; default HLANC_BASIS_AUTO */
-    int reserved[4];
+    int cgs_kernel;           /* HLANC_CGS_*; default HLANC_CGS_AUTO */
+    int reserved[3];
 } hlanc_opts_t;
 
 /* Fill defaults (tol 0, max_restarts 200, FP64, seed 0, graphs on, host restart). */

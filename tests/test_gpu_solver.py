@@ -263,6 +263,71 @@ def test_basis_fp64_path_beyond_tensor_core_shape(H):
     _check_pairs(m, vals, vecs, 20)
 
 
+@pytest.mark.parametrize("case,gen,nev,ncv", [
+    ("c1_laplacian2d_100", lambda: G.laplacian_2d(100), 10, 30),
+    ("lap3d_12_shift", lambda: G.laplacian_3d(12, shift_seed=1), 20, 60),
+    ("banded_3000_bw5", lambda: G.banded_random(3000, 5, seed=3, problem=0), 8, 24),
+    ("chunglu_4096", lambda: G.chung_lu_normalized(4096, seed=2), 16, 48),
+])
+def test_hybrid_cgs_matches_reference(H, case, gen, nev, ncv):
+    # the hybrid CGS kernels (part of every column panel as exact fixed-point
+    # integer products) forced at sizes where the default keeps FP64
+    g = golden(f"{case}.npz")
+    m = gen()
+    op = H.dcsrmv_operator_gpu(m)
+    rc, vals, vecs, st = H.solve(op, nev, ncv, seed=int(g["seed"]), cgs=H.HLANC_CGS_HYBRID)
+    assert rc == 0, st
+    assert st["nconv"] >= nev
+    ref = g["values"]
+    assert np.abs(vals[:nev] - ref).max() <= EV_RTOL * np.abs(ref).max()
+    _check_pairs(m, vals, vecs, nev)
+
+
+def _anderson(n, scale, seed=5):
+    # random diagonal U(-1, 1) with nearest-neighbour coupling -0.05: the top
+    # eigenvectors are localised (entries from ~1 down to ~1e-20)
+    rng = np.random.default_rng(seed)
+    d = rng.uniform(-1.0, 1.0, n) * scale
+    rp, ci, va = [0], [], []
+    for i in range(n):
+        for j, x in ((i - 1, -0.05 * scale), (i, d[i]), (i + 1, -0.05 * scale)):
+            if 0 <= j < n:
+                ci.append(j)
+                va.append(x)
+        rp.append(len(ci))
+    return G.CSR(n, n, np.array(rp, dtype=np.int32), np.array(ci, dtype=np.int32), np.array(va))
+
+
+@pytest.mark.parametrize("scale", [1e-150, 1.0, 1e150])
+def test_hybrid_cgs_localised_and_scaled(H, scale):
+    # localised basis vectors at extreme operator norms: the fixed-point
+    # scales follow w and h, and hybrid and FP64 CGS give the same pairs to
+    # FP64-level accuracy.  (At 1e-150 the reference's convergence floor
+    # eps * eps^(2/3) is absolute, so the solve stops after one restart and
+    # only the agreement of the two kernels is checked.)
+    m = _anderson(2000, scale)
+    op = H.dcsrmv_operator_gpu(m)
+    rc1, v1, x1, s1 = H.solve(op, 6, 24, cgs=H.HLANC_CGS_HYBRID)
+    rc2, v2, x2, s2 = H.solve(op, 6, 24, cgs=H.HLANC_CGS_FP64)
+    assert rc1 == rc2 == 0
+    assert np.abs(v1[:6] - v2[:6]).max() <= 1e-12 * np.abs(v2[:6]).max()
+    if scale >= 1.0:
+        _check_pairs(m, v1, x1, 6)
+        ref = np.linalg.eigvalsh(G.to_scipy(m).toarray())[-6:]
+        assert np.abs(v1[:6] - ref).max() <= EV_RTOL * np.abs(ref).max()
+
+
+def test_hybrid_cgs_default_on_large_problem(H):
+    # 2^18 rows: the default picks the hybrid kernels; same pairs as FP64
+    m = G.chung_lu_normalized(2 ** 18, seed=2)
+    op = H.dcsrmv_operator_gpu(m)
+    rc1, v1, x1, s1 = H.solve(op, 8, 24, tol=1e-10)
+    rc2, v2, x2, s2 = H.solve(op, 8, 24, tol=1e-10, cgs=H.HLANC_CGS_FP64)
+    assert rc1 == rc2 == 0
+    assert np.abs(v1[:8] - v2[:8]).max() <= 1e-12 * np.abs(v2[:8]).max()
+    _check_pairs(m, v1, x1, 8)
+
+
 def test_native_library_loaded(H):
     import os
     with open("/proc/self/maps") as f:
