@@ -124,6 +124,7 @@ def _declare(L):
         "hlanc_eigs_read": (_i, [C.c_char_p, _p, _p, _i]),
         "hlanc_last_profile": (_i, [C.POINTER(Profile)]),
         "hlanc_diag_fp64_tflops": (_i, [_i, C.POINTER(C.c_double)]),
+        "hlanc_diag_cgs": (_i, [_i, _i, _i, _i, _i, C.POINTER(C.c_double)]),
         "hlanc_batch_create": (_i, [_i, _i, _p, _p, _p, C.POINTER(Opts), C.POINTER(_p)]),
         "hlanc_batch_run": (_i, [_p, _p, _p, _p, C.POINTER(Stats)]),
         "hlanc_batch_destroy": (_i, [_p]),
@@ -414,6 +415,14 @@ def fp64_peak_tflops(dev: int = 0) -> float:
     t = C.c_double()
     _check(lib().hlanc_diag_fp64_tflops(dev, C.byref(t)), "fp64 probe")
     return t.value
+
+
+def cgs_kernel_ms(n: int, c: int, cgs: int = HLANC_CGS_HYBRID, reps: int = 10, dev: int = 0) -> dict:
+    """The CGS kernels alone on a synthetic n x c basis: mean ms per launch of
+    a first-pass projection, a second-pass projection and an update."""
+    ms = (C.c_double * 3)()
+    _check(lib().hlanc_diag_cgs(dev, n, c, cgs, reps, ms), "cgs probe")
+    return {"proj_pass1": ms[0], "proj": ms[1], "apply": ms[2]}
 
 
 def last_profile() -> dict:

@@ -308,6 +308,9 @@ public:
     bool basis_tc = true;                // basis update on the tensor cores when the shape fits
     int cgs_mode = HLANC_CGS_AUTO;       // CGS panels split between the FP64 and the integer pipes
     long long rows_active = 0;           // rows of all problems in the launch tables
+    Problem one_h;                       // descriptor of a single-problem launch table
+    int one_tr = 0;                      // its tile rows (0: several problems)
+    const Problem *one() const { return one_tr > 0 ? &one_h : nullptr; }
     std::vector<ProbRes> probs;
     std::vector<int> active;             // problems in the launch tables, in slot order
     Problem *P_d = nullptr;
@@ -469,6 +472,11 @@ public:
         nstiles = (int)ST.size();
         if (!ST.empty()) CK(cudaMemcpyAsync(S_d, ST.data(), sizeof(SpmvTile) * ST.size(), cudaMemcpyHostToDevice, stream));
         ntiles = (int)T.size();
+        one_tr = 0;
+        if (active.size() == 1) {
+            one_h = P[0];
+            one_tr = probs[active[0]].tr;
+        }
         if (!P.empty()) CK(cudaMemcpyAsync(P_d, P.data(), sizeof(Problem) * P.size(), cudaMemcpyHostToDevice, stream));
         if (!T.empty()) CK(cudaMemcpyAsync(T_d, T.data(), sizeof(Tile) * T.size(), cudaMemcpyHostToDevice, stream));
         if (!active.empty())
@@ -514,7 +522,8 @@ public:
         const int na = (int)active.size();
         if (!device_restart) launch_scatter(P_d, na, off_d, flag_d, mbox_d, stream);
         if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), basis_tc, stream);
-        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, hybrid_cgs(), stream);
+        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, hybrid_cgs(), one(), one_tr,
+                                                    stream);
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
     }
@@ -609,7 +618,7 @@ public:
             if (p.host_op(p.host_ctx, xs_h, ys_h) != 0) return HLANC_ERR_CALLBACK;
             double *w = ((j + 1) & 1) ? p.r1 : p.r0;
             CK(cudaMemcpyAsync(w, ys_h, sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
-            launch_step(P_d, T_d, ntiles, S_d, nstiles, s, false, true, hybrid_cgs(), stream);
+            launch_step(P_d, T_d, ntiles, S_d, nstiles, s, false, true, hybrid_cgs(), one(), one_tr, stream);
         }
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
@@ -1315,6 +1324,63 @@ int hlanc_eigs_read(const char *filename, double *values, double *vectors, int l
     return HLANC_OK;
 }
 
+// ---- diagnostics: the CGS kernels alone ----------------------------------------------
+static int diag_no_op(void *, const double *, double *) { return 1; }
+
+int hlanc_diag_cgs(int dev, int n, int c, int cgs_kernel, int reps, double *ms3) {
+    if (n < 1024 || c < 2 || c > HLANC_MAX_NCV || reps < 1 || !ms3) return HLANC_ERR_INVALID;
+    if (cgs_kernel != HLANC_CGS_FP64 && cgs_kernel != HLANC_CGS_HYBRID) return HLANC_ERR_INVALID;
+    DevGuard g(dev);
+    Engine E;
+    int rc = E.init(dev, nullptr, false, false);
+    if (rc) return rc;
+    hlanc_opts_t o;
+    hlanc_opts_default(&o);
+    int idx = -1;
+    rc = E.add(n, 1, c, nullptr, diag_no_op, nullptr, 0, o, &idx);
+    if (rc) return rc;
+    E.active.assign(1, idx);
+    rc = E.upload();
+    if (rc) return rc;
+    ProbRes &p = E.probs[idx];
+    // basis entries U(-1,1) sqrt(3/n) (columns of norm ~1), w entries U(-1,1)
+    launch_diag_fill(p.V, (size_t)p.ld * c, sqrt(3.0 / n), 11, E.stream);
+    launch_diag_fill(p.r0, (size_t)p.ld, 1.0, 12, E.stream);
+    launch_diag_fill(p.r1, (size_t)p.ld, 1.0, 13, E.stream);
+    // step 0 of an extension at j = c - 1 (c basis columns), second pass flagged
+    State S = p.hs;
+    S.status = ST_RUNNING;
+    S.phase = PH_EXTEND;
+    S.k = c - 1;
+    S.np = 1;
+    S.iter = 0;
+    S.need2 = 1;
+    S.need3 = 0;
+    S.rnorm = S.wnorm = sqrt((double)n);
+    CK(cudaMemcpyAsync(p.st, &S, sizeof S, cudaMemcpyHostToDevice, E.stream));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const bool hy = cgs_kernel == HLANC_CGS_HYBRID;
+    const int pass_of[3] = {1, 2, 2}, which_of[3] = {0, 0, 1};
+    for (int q = 0; q < 3; ++q) {
+        for (int w = 0; w < 2; ++w)
+            launch_cgs_kernel(E.P_d, E.T_d, E.ntiles, E.one(), E.one_tr, 0, pass_of[q], which_of[q], hy, E.stream);
+        CK(cudaEventRecord(e0, E.stream));
+        for (int r = 0; r < reps; ++r)
+            launch_cgs_kernel(E.P_d, E.T_d, E.ntiles, E.one(), E.one_tr, 0, pass_of[q], which_of[q], hy, E.stream);
+        CK(cudaEventRecord(e1, E.stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        ms3[q] = ms / reps;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaGetLastError());
+    return HLANC_OK;
+}
+
 // ---- batched solves ------------------------------------------------------------------
 }  // extern "C"
 
@@ -1751,7 +1817,8 @@ int srv_launch(Srv &s, Srv::Lane &L) {
     if (basis_nev > 0)
         launch_basis(E.P_d, E.T_d, E.ntiles, E.max_ncv, Engine::basis_bucket(basis_nev), E.basis_tc, E.stream);
     for (int k = 0; k < steps; ++k)
-        launch_step(E.P_d, E.T_d, E.ntiles, E.S_d, E.nstiles, k, E.fp32_any, false, E.hybrid_cgs(), E.stream);
+        launch_step(E.P_d, E.T_d, E.ntiles, E.S_d, E.nstiles, k, E.fp32_any, false, E.hybrid_cgs(), E.one(),
+                    E.one_tr, E.stream);
     launch_gather(E.P_d, na, E.off_d, E.mbox_d, E.stream);
     if ((rc = E.pull_async())) return rc;
     CK(cudaEventRecord(L.ev1, E.stream));

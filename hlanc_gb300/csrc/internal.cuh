@@ -244,8 +244,12 @@ void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, in
                          unsigned long long seed, cudaStream_t s);
 void launch_norm_init(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s);
 void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const SpmvTile *stiles_d,
-                 int nstiles, int step, bool fp32_any, bool external_w, bool cgs_hybrid, cudaStream_t s);
+                 int nstiles, int step, bool fp32_any, bool external_w, bool cgs_hybrid, const Problem *one,
+                 int one_tr, cudaStream_t s);
 void launch_prep_f32(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, cudaStream_t s);
+void launch_diag_fill(double *x, size_t count, double scale, unsigned long long key, cudaStream_t s);
+void launch_cgs_kernel(const Problem *P_d, const Tile *tiles_d, int ntiles, const Problem *one, int one_tr,
+                       int step, int pass, int which, bool hybrid, cudaStream_t s);
 void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, double *xout,
                      cudaStream_t s);
 void launch_restart(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);

@@ -14,6 +14,7 @@
 // exactly one DFMA per loaded element and every reduction is accumulated in
 // registers over a whole tile before the (few) shuffle additions.
 #include <float.h>
+#include <string.h>
 
 #include <type_traits>
 
@@ -247,10 +248,9 @@ __global__ void __launch_bounds__(TPB) k_prep(const Problem *__restrict__ probs,
 // w's fixed-point scale is the largest exponent of the thread's own rows on
 // pass 1 (one extra read of w, which also gives ||w||^2) and 2 ||w|| on
 // later passes (||w|| is known from the previous k_apply).
-template <int ND, int NI>
+template <int ND, int NI, bool with_norm = false>
 __device__ __forceinline__ void proj_panel(const double *__restrict__ V, size_t ld, int row0, int row1,
-                                           const double *__restrict__ w, int c0, int ew, bool with_norm,
-                                           double *red, double *sm) {
+                                           const double *__restrict__ w, int c0, int ew, double *red, double *sm) {
     constexpr int NC = ND + NI;
     static_assert(NC >= 1 && NC <= 8, "panel width");
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -266,7 +266,7 @@ __device__ __forceinline__ void proj_panel(const double *__restrict__ V, size_t 
     const double *__restrict__ vc = V + (size_t)c0 * ld;
     for (int r = row0 + (int)threadIdx.x; r < row1; r += TPB) {
         const double wr = w[r];
-        if (with_norm) nrm = fma(wr, wr, nrm);
+        if constexpr (with_norm) nrm = fma(wr, wr, nrm);
         const double *__restrict__ vr = vc + r;
 #pragma unroll
         for (int k = 0; k < ND; ++k) acc[k] = fma(__ldcs(vr + (size_t)k * ld), wr, acc[k]);
@@ -294,7 +294,7 @@ __device__ __forceinline__ void proj_panel(const double *__restrict__ V, size_t 
         const double v = warp_reduce8(acc);
         if ((lane & 3) == 0) sm[warp * 8 + (lane >> 2)] = v;
     }
-    if (with_norm) {
+    if constexpr (with_norm) {
         nrm = warp_sum(nrm);
         if (lane == 0) sm[8 * 8 + warp] = nrm;
     }
@@ -312,18 +312,18 @@ __device__ __forceinline__ void proj_panel(const double *__restrict__ V, size_t 
     __syncthreads();
 }
 
+template <bool NORM>
 __device__ __forceinline__ void proj_panel_fp64(const double *__restrict__ V, size_t ld, int row0, int row1,
-                                                const double *__restrict__ w, int c0, int cc, bool nrm,
-                                                double *red, double *sm) {
+                                                const double *__restrict__ w, int c0, int cc, double *red,
+                                                double *sm) {
     switch (cc) {
-    case 1: proj_panel<1, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
-    case 2: proj_panel<2, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
-    case 3: proj_panel<3, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
-    case 4: proj_panel<4, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
-    case 5: proj_panel<5, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
-    case 6: proj_panel<6, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
-    case 7: proj_panel<7, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
-    default: proj_panel<8, 0>(V, ld, row0, row1, w, c0, 0, nrm, red, sm); break;
+    case 1: proj_panel<1, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 2: proj_panel<2, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 3: proj_panel<3, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 4: proj_panel<4, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 5: proj_panel<5, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 6: proj_panel<6, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    default: proj_panel<7, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
     }
 }
 
@@ -331,22 +331,44 @@ __device__ __forceinline__ void proj_panel_hybrid(const double *__restrict__ V, 
                                                   const double *__restrict__ w, int c0, int cc, int ew,
                                                   double *red, double *sm) {
     switch (cc) {
-    case 1: proj_panel<1, 0>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
-    case 2: proj_panel<1, 1>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
-    case 3: proj_panel<2, 1>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
-    case 4: proj_panel<2, 2>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
-    case 5: proj_panel<3, 2>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
-    case 6: proj_panel<3, 3>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
-    case 7: proj_panel<4, 3>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
-    default: proj_panel<5, 3>(V, ld, row0, row1, w, c0, ew, false, red, sm); break;
+    case 1: proj_panel<1, 0>(V, ld, row0, row1, w, c0, ew, red, sm); break;
+    case 2: proj_panel<1, 1>(V, ld, row0, row1, w, c0, ew, red, sm); break;
+    case 3: proj_panel<2, 1>(V, ld, row0, row1, w, c0, ew, red, sm); break;
+    case 4: proj_panel<2, 2>(V, ld, row0, row1, w, c0, ew, red, sm); break;
+    case 5: proj_panel<3, 2>(V, ld, row0, row1, w, c0, ew, red, sm); break;
+    case 6: proj_panel<3, 3>(V, ld, row0, row1, w, c0, ew, red, sm); break;
+    default: proj_panel<4, 3>(V, ld, row0, row1, w, c0, ew, red, sm); break;
     }
 }
 
-template <bool HY>
+// ONE: a launch over a single problem, whose descriptor is passed by value
+// (kernel parameter space, so the basis pointer and stride stay in uniform
+// registers) with tiles of tr rows in blockIdx order.  Measured on GB300
+// (4.1M rows, 32 columns): 207 us against 218 us for descriptor and tile
+// loads from the tables, which batched launches need.
+template <bool ONE>
+struct TileRows {
+    int row0, row1, prob;
+    __device__ __forceinline__ TileRows(const Tile *__restrict__ tiles, const Problem &P1, int tr) {
+        if constexpr (ONE) {
+            row0 = blockIdx.x * tr;
+            row1 = min(P1.n, row0 + tr);
+            prob = 0;
+        } else {
+            const Tile t = tiles[blockIdx.x];
+            row0 = t.row0;
+            row1 = t.row1;
+            prob = t.prob;
+        }
+    }
+};
+
+template <bool HY, bool ONE>
 __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ probs,
-                                              const Tile *__restrict__ tiles, int s, int pass) {
-    const Tile t = tiles[blockIdx.x];
-    const Problem &P = probs[t.prob];
+                                              const Tile *__restrict__ tiles, const Problem P1, int tr,
+                                              int s, int pass) {
+    const TileRows<ONE> t(tiles, P1, tr);
+    const Problem &P = ONE ? P1 : probs[t.prob];
     State *S = P.st;
     if (!step_active(S, s)) return;
     if ((pass == 2 && !S->need2) || (pass == 3 && !S->need3)) return;
@@ -376,12 +398,21 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
         } else {
             ew = fx_scale(fx_hi_abs(S->rnorm)) + 1;   // |w_i| <= ||w|| < 2^(ew + 1)
         }
-        for (int c0 = 0; c0 < c; c0 += 8)
-            proj_panel_hybrid(V, ld, t.row0, t.row1, w, c0, min(8, c - c0), ew, red, sm);
+        // full panels called directly (a switch around every panel measured
+        // 5% slower), then the remainder
+        int c0 = 0;
+        for (; c0 + 8 <= c; c0 += 8) proj_panel<5, 3>(V, ld, t.row0, t.row1, w, c0, ew, red, sm);
+        if (c0 < c) proj_panel_hybrid(V, ld, t.row0, t.row1, w, c0, c - c0, ew, red, sm);
     } else {
-        for (int c0 = 0; c0 < c; c0 += 8) {
-            const int cc = min(8, c - c0);
-            proj_panel_fp64(V, ld, t.row0, t.row1, w, c0, cc, pass == 1 && c0 + cc == c, red, sm);
+        // ||w||^2 rides with the last panel on pass 1
+        int c0 = 0;
+        for (; c0 + 8 <= c; c0 += 8) {
+            if (pass == 1 && c0 + 8 == c) proj_panel<8, 0, true>(V, ld, t.row0, t.row1, w, c0, 0, red, sm);
+            else proj_panel<8, 0>(V, ld, t.row0, t.row1, w, c0, 0, red, sm);
+        }
+        if (c0 < c) {
+            if (pass == 1) proj_panel_fp64<true>(V, ld, t.row0, t.row1, w, c0, c - c0, red, sm);
+            else proj_panel_fp64<false>(V, ld, t.row0, t.row1, w, c0, c - c0, red, sm);
         }
     }
     __syncthreads();
@@ -409,11 +440,12 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
 // Measured on GB300 (n = 4.1M, 32 columns): 186 us against 245 us for the
 // all-FP64 loop; interleaving 4 + 4 columns inside every group of 8 was no
 // faster than all-FP64 in the solver.
-template <bool HY>
+template <bool HY, bool ONE>
 __global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__restrict__ probs,
-                                               const Tile *__restrict__ tiles, int s, int pass) {
-    const Tile t = tiles[blockIdx.x];
-    const Problem &P = probs[t.prob];
+                                               const Tile *__restrict__ tiles, const Problem P1, int tr,
+                                               int s, int pass) {
+    const TileRows<ONE> t(tiles, P1, tr);
+    const Problem &P = ONE ? P1 : probs[t.prob];
     State *S = P.st;
     if (!step_active(S, s)) return;
     if ((pass == 2 && !S->need2) || (pass == 3 && !S->need3)) return;
@@ -630,7 +662,8 @@ void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int st
 // One Lanczos step for every active problem of the tile table.  With
 // external_w the operator output was already written by the host path.
 void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const SpmvTile *stiles_d,
-                 int nstiles, int step, bool fp32_any, bool external_w, bool cgs_hybrid, cudaStream_t s) {
+                 int nstiles, int step, bool fp32_any, bool external_w, bool cgs_hybrid, const Problem *one,
+                 int one_tr, cudaStream_t s) {
     if (!external_w) {
         if (fp32_any) {
             prof_begin(s);
@@ -648,15 +681,46 @@ void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const Spmv
     }
     for (int pass = 1; pass <= 3; ++pass) {
         prof_begin(s);
-        if (cgs_hybrid) k_proj<true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
-        else k_proj<false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+        launch_cgs_kernel(P_d, tiles_d, ntiles, one, one_tr, step, pass, 0, cgs_hybrid, s);
         prof_end(KC_PROJ, s);
         prof_begin(s);
-        if (cgs_hybrid) k_apply<true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
-        else k_apply<false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, pass);
+        launch_cgs_kernel(P_d, tiles_d, ntiles, one, one_tr, step, pass, 1, cgs_hybrid, s);
         prof_end(KC_APPLY, s);
     }
-    launch_counter() += 6;
+}
+
+// ---- diagnostics: one CGS kernel alone (hlanc_diag_cgs) -----------------------
+__global__ void k_diag_fill(double *__restrict__ x, size_t count, double scale, unsigned long long key) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+        const uint64_t z = sm_mix(key + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ULL);
+        x[i] = scale * (2.0 * ((double)(z >> 11) * 0x1.0p-53) - 1.0);
+    }
+}
+
+void launch_diag_fill(double *x, size_t count, double scale, unsigned long long key, cudaStream_t s) {
+    k_diag_fill<<<1216, 256, 0, s>>>(x, count, scale, key);
+    launch_counter() += 1;
+}
+
+// which: 0 = projection, 1 = update.  one: the host copy of the descriptor
+// of a single-problem launch (tiles of one_tr rows), or null.
+void launch_cgs_kernel(const Problem *P_d, const Tile *tiles_d, int ntiles, const Problem *one, int one_tr,
+                       int step, int pass, int which, bool hybrid, cudaStream_t s) {
+    Problem P1;
+    if (one) P1 = *one;
+    else memset(&P1, 0, sizeof P1);
+    const int code = (which << 2) | (hybrid ? 2 : 0) | (one ? 1 : 0);
+    switch (code) {
+    case 0: k_proj<false, false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 1: k_proj<false, true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 2: k_proj<true, false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 3: k_proj<true, true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 4: k_apply<false, false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 5: k_apply<false, true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 6: k_apply<true, false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
+    default: k_apply<true, true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
+    }
+    launch_counter() += 1;
 }
 
 void launch_spmv(const int *row_ptr, const int *col, const double *val, const SpmvTile *stiles, int nstiles,

@@ -265,6 +265,11 @@ int hlanc_last_profile(hlanc_profile_t *out);
 /* Measured dense FP64 FMA throughput of device `dev` (TFLOP/s): the ceiling
  * of kernels that issue one FP64 FMA per loaded 8-byte element. */
 int hlanc_diag_fp64_tflops(int dev, double *tflops);
+/* The CGS kernels alone on a synthetic basis of n rows and c columns
+ * (cgs_kernel HLANC_CGS_FP64 or HLANC_CGS_HYBRID), each launched reps times
+ * back to back: ms3 = mean ms of a first-pass projection (with ||w||),
+ * a second-pass projection and a second-pass update. */
+int hlanc_diag_cgs(int dev, int n, int c, int cgs_kernel, int reps, double *ms3);
 
 #ifdef __cplusplus
 }
