@@ -252,11 +252,12 @@ template <int ND, int NI, bool with_norm = false>
 __device__ __forceinline__ void proj_panel(const double *__restrict__ V, size_t ld, int row0, int row1,
                                            const double *__restrict__ w, int c0, int ew, double *red, double *sm) {
     constexpr int NC = ND + NI;
-    static_assert(NC >= 1 && NC <= 8, "panel width");
+    constexpr int NA = (NC + 7) / 8 * 8;
+    static_assert(NC >= 1 && NC <= 16 && (NI == 0 || NC <= 8), "panel width");
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double acc[8];
+    double acc[NA];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) acc[i] = 0.0;
+    for (int i = 0; i < NA; ++i) acc[i] = 0.0;
     FxAcc A[NI > 0 ? NI : 1];
 #pragma unroll
     for (int i = 0; i < NI; ++i) fx_zero(A[i]);
@@ -289,24 +290,25 @@ __device__ __forceinline__ void proj_panel(const double *__restrict__ V, size_t 
     // products carry the scales 2^57 (V) and 2^(57 - ew) (w)
 #pragma unroll
     for (int k = 0; k < NI; ++k) acc[ND + k] = fx_to_double(A[k], ew - 114);
-    // lane l holds the warp sum of column l >> 2
-    {
-        const double v = warp_reduce8(acc);
-        if ((lane & 3) == 0) sm[warp * 8 + (lane >> 2)] = v;
+    // lane l holds, per group g of 8 columns, the warp sum of column 8g + (l >> 2)
+#pragma unroll
+    for (int g = 0; g < NA / 8; ++g) {
+        const double v = warp_reduce8(acc + 8 * g);
+        if ((lane & 3) == 0) sm[warp * 16 + 8 * g + (lane >> 2)] = v;
     }
     if constexpr (with_norm) {
         nrm = warp_sum(nrm);
-        if (lane == 0) sm[8 * 8 + warp] = nrm;
+        if (lane == 0) sm[16 * 8 + warp] = nrm;
     }
     __syncthreads();
     if (threadIdx.x < NC) {
         double s = 0.0;
-        for (int q = 0; q < TPB / 32; ++q) s += sm[q * 8 + threadIdx.x];
+        for (int q = 0; q < TPB / 32; ++q) s += sm[q * 16 + threadIdx.x];
         red[c0 + threadIdx.x] = s;
     }
     if (with_norm && threadIdx.x == 32) {
         double s = 0.0;
-        for (int q = 0; q < TPB / 32; ++q) s += sm[8 * 8 + q];
+        for (int q = 0; q < TPB / 32; ++q) s += sm[16 * 8 + q];
         red[c0 + NC] = s;
     }
     __syncthreads();
@@ -323,7 +325,15 @@ __device__ __forceinline__ void proj_panel_fp64(const double *__restrict__ V, si
     case 4: proj_panel<4, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
     case 5: proj_panel<5, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
     case 6: proj_panel<6, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    default: proj_panel<7, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 7: proj_panel<7, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 8: proj_panel<8, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 9: proj_panel<9, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 10: proj_panel<10, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 11: proj_panel<11, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 12: proj_panel<12, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 13: proj_panel<13, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 14: proj_panel<14, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    default: proj_panel<15, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
     }
 }
 
@@ -379,7 +389,7 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
     const double *__restrict__ V = P.V;
     const size_t ld = (size_t)P.ld;
     __shared__ double red[MAXNCV + 1], tot[MAXNCV + 1];
-    __shared__ double sm[9 * 8 + 32];
+    __shared__ double sm[17 * 8];
     if constexpr (HY) {
         int ew;
         if (pass == 1) {
@@ -404,11 +414,12 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
         for (; c0 + 8 <= c; c0 += 8) proj_panel<5, 3>(V, ld, t.row0, t.row1, w, c0, ew, red, sm);
         if (c0 < c) proj_panel_hybrid(V, ld, t.row0, t.row1, w, c0, c - c0, ew, red, sm);
     } else {
-        // ||w||^2 rides with the last panel on pass 1
+        // 16-column panels (measured fastest for the FP64 kernel: 64
+        // registers, 4 CTAs per SM); ||w||^2 rides with the last panel on pass 1
         int c0 = 0;
-        for (; c0 + 8 <= c; c0 += 8) {
-            if (pass == 1 && c0 + 8 == c) proj_panel<8, 0, true>(V, ld, t.row0, t.row1, w, c0, 0, red, sm);
-            else proj_panel<8, 0>(V, ld, t.row0, t.row1, w, c0, 0, red, sm);
+        for (; c0 + 16 <= c; c0 += 16) {
+            if (pass == 1 && c0 + 16 == c) proj_panel<16, 0, true>(V, ld, t.row0, t.row1, w, c0, 0, red, sm);
+            else proj_panel<16, 0>(V, ld, t.row0, t.row1, w, c0, 0, red, sm);
         }
         if (c0 < c) {
             if (pass == 1) proj_panel_fp64<true>(V, ld, t.row0, t.row1, w, c0, c - c0, red, sm);
