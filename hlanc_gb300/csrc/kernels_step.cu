@@ -248,9 +248,15 @@ __global__ void __launch_bounds__(TPB) k_prep(const Problem *__restrict__ probs,
 // w's fixed-point scale is the largest exponent of the thread's own rows on
 // pass 1 (one extra read of w, which also gives ||w||^2) and 2 ||w|| on
 // later passes (||w|| is known from the previous k_apply).
+// Warp sums of every panel go to wsum[warp * WSTRIDE + column] without a
+// barrier; one cross-warp sum after the last panel (proj_combine).  Measured
+// on GB300: a cross-warp reduction with two barriers per panel left every
+// warp waiting for the slowest at each panel boundary.
+constexpr int WSTRIDE = MAXNCV + 1;
+
 template <int ND, int NI, bool with_norm = false>
 __device__ __forceinline__ void proj_panel(const double *__restrict__ V, size_t ld, int row0, int row1,
-                                           const double *__restrict__ w, int c0, int ew, double *red, double *sm) {
+                                           const double *__restrict__ w, int c0, int ew, double *wsum) {
     constexpr int NC = ND + NI;
     constexpr int NA = (NC + 7) / 8 * 8;
     static_assert(NC >= 1 && NC <= 16 && (NI == 0 || NC <= 8), "panel width");
@@ -291,63 +297,64 @@ __device__ __forceinline__ void proj_panel(const double *__restrict__ V, size_t 
 #pragma unroll
     for (int k = 0; k < NI; ++k) acc[ND + k] = fx_to_double(A[k], ew - 114);
     // lane l holds, per group g of 8 columns, the warp sum of column 8g + (l >> 2)
+    double *ws = wsum + warp * WSTRIDE + c0;
 #pragma unroll
     for (int g = 0; g < NA / 8; ++g) {
         const double v = warp_reduce8(acc + 8 * g);
-        if ((lane & 3) == 0) sm[warp * 16 + 8 * g + (lane >> 2)] = v;
+        const int q = 8 * g + (lane >> 2);
+        if ((lane & 3) == 0 && q < NC) ws[q] = v;
     }
     if constexpr (with_norm) {
         nrm = warp_sum(nrm);
-        if (lane == 0) sm[16 * 8 + warp] = nrm;
+        if (lane == 0) ws[NC] = nrm;
     }
+}
+
+// red[i] = sum over the warps of wsum[warp][i], i < nv, in warp order
+__device__ __forceinline__ void proj_combine(const double *wsum, int nv, double *red) {
     __syncthreads();
-    if (threadIdx.x < NC) {
+    for (int i = threadIdx.x; i < nv; i += TPB) {
         double s = 0.0;
-        for (int q = 0; q < TPB / 32; ++q) s += sm[q * 16 + threadIdx.x];
-        red[c0 + threadIdx.x] = s;
-    }
-    if (with_norm && threadIdx.x == 32) {
-        double s = 0.0;
-        for (int q = 0; q < TPB / 32; ++q) s += sm[16 * 8 + q];
-        red[c0 + NC] = s;
+#pragma unroll
+        for (int q = 0; q < TPB / 32; ++q) s += wsum[q * WSTRIDE + i];
+        red[i] = s;
     }
     __syncthreads();
 }
 
 template <bool NORM>
 __device__ __forceinline__ void proj_panel_fp64(const double *__restrict__ V, size_t ld, int row0, int row1,
-                                                const double *__restrict__ w, int c0, int cc, double *red,
-                                                double *sm) {
+                                                const double *__restrict__ w, int c0, int cc, double *wsum) {
     switch (cc) {
-    case 1: proj_panel<1, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 2: proj_panel<2, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 3: proj_panel<3, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 4: proj_panel<4, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 5: proj_panel<5, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 6: proj_panel<6, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 7: proj_panel<7, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 8: proj_panel<8, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 9: proj_panel<9, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 10: proj_panel<10, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 11: proj_panel<11, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 12: proj_panel<12, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 13: proj_panel<13, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    case 14: proj_panel<14, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
-    default: proj_panel<15, 0, NORM>(V, ld, row0, row1, w, c0, 0, red, sm); break;
+    case 1: proj_panel<1, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 2: proj_panel<2, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 3: proj_panel<3, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 4: proj_panel<4, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 5: proj_panel<5, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 6: proj_panel<6, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 7: proj_panel<7, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 8: proj_panel<8, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 9: proj_panel<9, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 10: proj_panel<10, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 11: proj_panel<11, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 12: proj_panel<12, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 13: proj_panel<13, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    case 14: proj_panel<14, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
+    default: proj_panel<15, 0, NORM>(V, ld, row0, row1, w, c0, 0, wsum); break;
     }
 }
 
 __device__ __forceinline__ void proj_panel_hybrid(const double *__restrict__ V, size_t ld, int row0, int row1,
                                                   const double *__restrict__ w, int c0, int cc, int ew,
-                                                  double *red, double *sm) {
+                                                  double *wsum) {
     switch (cc) {
-    case 1: proj_panel<1, 0>(V, ld, row0, row1, w, c0, ew, red, sm); break;
-    case 2: proj_panel<1, 1>(V, ld, row0, row1, w, c0, ew, red, sm); break;
-    case 3: proj_panel<2, 1>(V, ld, row0, row1, w, c0, ew, red, sm); break;
-    case 4: proj_panel<2, 2>(V, ld, row0, row1, w, c0, ew, red, sm); break;
-    case 5: proj_panel<3, 2>(V, ld, row0, row1, w, c0, ew, red, sm); break;
-    case 6: proj_panel<3, 3>(V, ld, row0, row1, w, c0, ew, red, sm); break;
-    default: proj_panel<4, 3>(V, ld, row0, row1, w, c0, ew, red, sm); break;
+    case 1: proj_panel<1, 0>(V, ld, row0, row1, w, c0, ew, wsum); break;
+    case 2: proj_panel<1, 1>(V, ld, row0, row1, w, c0, ew, wsum); break;
+    case 3: proj_panel<2, 1>(V, ld, row0, row1, w, c0, ew, wsum); break;
+    case 4: proj_panel<2, 2>(V, ld, row0, row1, w, c0, ew, wsum); break;
+    case 5: proj_panel<3, 2>(V, ld, row0, row1, w, c0, ew, wsum); break;
+    case 6: proj_panel<3, 3>(V, ld, row0, row1, w, c0, ew, wsum); break;
+    default: proj_panel<4, 3>(V, ld, row0, row1, w, c0, ew, wsum); break;
     }
 }
 
@@ -389,7 +396,8 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
     const double *__restrict__ V = P.V;
     const size_t ld = (size_t)P.ld;
     __shared__ double red[MAXNCV + 1], tot[MAXNCV + 1];
-    __shared__ double sm[17 * 8];
+    __shared__ double sm[32];
+    __shared__ double wsum[(TPB / 32) * WSTRIDE];
     if constexpr (HY) {
         int ew;
         if (pass == 1) {
@@ -411,20 +419,22 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
         // full panels called directly (a switch around every panel measured
         // 5% slower), then the remainder
         int c0 = 0;
-        for (; c0 + 8 <= c; c0 += 8) proj_panel<5, 3>(V, ld, t.row0, t.row1, w, c0, ew, red, sm);
-        if (c0 < c) proj_panel_hybrid(V, ld, t.row0, t.row1, w, c0, c - c0, ew, red, sm);
+        for (; c0 + 8 <= c; c0 += 8) proj_panel<5, 3>(V, ld, t.row0, t.row1, w, c0, ew, wsum);
+        if (c0 < c) proj_panel_hybrid(V, ld, t.row0, t.row1, w, c0, c - c0, ew, wsum);
+        proj_combine(wsum, c, red);        // red[c] (pass 1) came from the scan
     } else {
         // 16-column panels (measured fastest for the FP64 kernel: 64
         // registers, 4 CTAs per SM); ||w||^2 rides with the last panel on pass 1
         int c0 = 0;
         for (; c0 + 16 <= c; c0 += 16) {
-            if (pass == 1 && c0 + 16 == c) proj_panel<16, 0, true>(V, ld, t.row0, t.row1, w, c0, 0, red, sm);
-            else proj_panel<16, 0>(V, ld, t.row0, t.row1, w, c0, 0, red, sm);
+            if (pass == 1 && c0 + 16 == c) proj_panel<16, 0, true>(V, ld, t.row0, t.row1, w, c0, 0, wsum);
+            else proj_panel<16, 0>(V, ld, t.row0, t.row1, w, c0, 0, wsum);
         }
         if (c0 < c) {
-            if (pass == 1) proj_panel_fp64<true>(V, ld, t.row0, t.row1, w, c0, c - c0, red, sm);
-            else proj_panel_fp64<false>(V, ld, t.row0, t.row1, w, c0, c - c0, red, sm);
+            if (pass == 1) proj_panel_fp64<true>(V, ld, t.row0, t.row1, w, c0, c - c0, wsum);
+            else proj_panel_fp64<false>(V, ld, t.row0, t.row1, w, c0, c - c0, wsum);
         }
+        proj_combine(wsum, c + (pass == 1 ? 1 : 0), red);
     }
     __syncthreads();
     if (!finish_tile(P, blockIdx.x - P.tile0, c + (pass == 1 ? 1 : 0), red, tot)) return;
