@@ -461,6 +461,61 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
 // Measured on GB300 (n = 4.1M, 32 columns): 186 us against 245 us for the
 // all-FP64 loop; interleaving 4 + 4 columns inside every group of 8 was no
 // faster than all-FP64 in the solver.
+// The last R < 8 columns of an update row, unrolled so that their loads
+// are issued together: FP64 FMAs, or exact integer products.
+template <int R>
+__device__ __forceinline__ double apply_tail_fp64(const double *__restrict__ vr, size_t ld, int k,
+                                                  const double *hs, double acc) {
+    double v[R > 0 ? R : 1];
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
+#pragma unroll
+    for (int q = 0; q < R; ++q) acc = fma(-v[q], hs[k + q], acc);
+    return acc;
+}
+
+template <int R>
+__device__ __forceinline__ void apply_tail_int(const double *__restrict__ vr, size_t ld, int k, const int *h1s,
+                                               const int *h0s, FxAcc &A) {
+    double v[R > 0 ? R : 1];
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        int x1, x0;
+        fx_split(v[q], FX_RS_UNIT, x1, x0);
+        fx_mac(A, x1, x0, h1s[k + q], h0s[k + q]);
+    }
+}
+
+__device__ __forceinline__ double apply_tail_fp64_n(const double *__restrict__ vr, size_t ld, int k, int r,
+                                                    const double *hs, double acc) {
+    switch (r) {
+    case 1: return apply_tail_fp64<1>(vr, ld, k, hs, acc);
+    case 2: return apply_tail_fp64<2>(vr, ld, k, hs, acc);
+    case 3: return apply_tail_fp64<3>(vr, ld, k, hs, acc);
+    case 4: return apply_tail_fp64<4>(vr, ld, k, hs, acc);
+    case 5: return apply_tail_fp64<5>(vr, ld, k, hs, acc);
+    case 6: return apply_tail_fp64<6>(vr, ld, k, hs, acc);
+    case 7: return apply_tail_fp64<7>(vr, ld, k, hs, acc);
+    default: return acc;
+    }
+}
+
+__device__ __forceinline__ void apply_tail_int_n(const double *__restrict__ vr, size_t ld, int k, int r,
+                                                 const int *h1s, const int *h0s, FxAcc &A) {
+    switch (r) {
+    case 1: apply_tail_int<1>(vr, ld, k, h1s, h0s, A); break;
+    case 2: apply_tail_int<2>(vr, ld, k, h1s, h0s, A); break;
+    case 3: apply_tail_int<3>(vr, ld, k, h1s, h0s, A); break;
+    case 4: apply_tail_int<4>(vr, ld, k, h1s, h0s, A); break;
+    case 5: apply_tail_int<5>(vr, ld, k, h1s, h0s, A); break;
+    case 6: apply_tail_int<6>(vr, ld, k, h1s, h0s, A); break;
+    case 7: apply_tail_int<7>(vr, ld, k, h1s, h0s, A); break;
+    default: break;
+    }
+}
+
 template <bool HY, bool ONE>
 __global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__restrict__ probs,
                                                const Tile *__restrict__ tiles, const Problem P1, int tr,
@@ -508,7 +563,10 @@ __global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__rest
 #pragma unroll
                 for (int q = 0; q < 8; ++q) acc = fma(-v[q], hs[k + q], acc);
             }
-            for (; k < cd; ++k) acc = fma(-__ldcs(vr + (size_t)k * ld), hs[k], acc);
+            if (k < cd) {           // only when c < 8 (cd = c)
+                acc = apply_tail_fp64_n(vr, ld, k, cd - k, hs, acc);
+                k = cd;
+            }
             if (k < c) {
                 FxAcc A;
                 fx_zero(A);
@@ -530,11 +588,7 @@ __global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__rest
                     }
                 }
                 // at most 7 more steps after 0 or 8: within the carry budget
-                for (; k < c; ++k) {
-                    int x1, x0;
-                    fx_split(__ldcs(vr + (size_t)k * ld), FX_RS_UNIT, x1, x0);
-                    fx_mac(A, x1, x0, h1s[k], h0s[k]);
-                }
+                apply_tail_int_n(vr, ld, k, c - k, h1s, h0s, A);
                 acc -= fx_to_double(A, eh - 114);
             }
         } else {
@@ -545,7 +599,7 @@ __global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__rest
 #pragma unroll
                 for (int q = 0; q < 8; ++q) acc = fma(-v[q], hs[k + q], acc);
             }
-            for (; k < c; ++k) acc = fma(-__ldcs(vr + (size_t)k * ld), hs[k], acc);
+            acc = apply_tail_fp64_n(vr, ld, k, c - k, hs, acc);
         }
         w[r] = acc;
         nrm = fma(acc, acc, nrm);
