@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(TPB, SPMV_CTAS_PER_SM) k_spmv_step(const Probl
     __shared__ int s_col[(TPB / 32) * STAGE];
     __shared__ T s_val[(TPB / 32) * STAGE];
     __shared__ T red[TPB / 32];
+    pdl_wait();
     const SpmvTile t = tiles[blockIdx.x];
     const Problem &P = probs[t.prob];
     const State *S = P.st;
@@ -204,12 +205,14 @@ __global__ void __launch_bounds__(TPB, SPMV_CTAS_PER_SM) k_spmv_step(const Probl
         spmv_unit<double>(t, P.row_ptr, P.col, P.val, rin, s_col, s_val, red,
                           [=](int rr, double acc) { w[rr] = scale ? acc * t1 : acc; });
     }
+    pdl_trigger();
 }
 
 // v_j -> V[:, j] (and its FP32 copy) ahead of an FP32 SpMV or a host operator.
 __global__ void __launch_bounds__(TPB) k_prep(const Problem *__restrict__ probs,
                                               const Tile *__restrict__ tiles, int s, int ext,
                                               double *__restrict__ xout) {
+    pdl_wait();
     const Tile t = tiles[blockIdx.x];
     const Problem &P = probs[t.prob];
     const State *S = P.st;
@@ -384,6 +387,7 @@ template <bool HY, bool ONE>
 __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ probs,
                                               const Tile *__restrict__ tiles, const Problem P1, int tr,
                                               int s, int pass) {
+    pdl_wait();
     const TileRows<ONE> t(tiles, P1, tr);
     const Problem &P = ONE ? P1 : probs[t.prob];
     State *S = P.st;
@@ -421,6 +425,7 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
         int c0 = 0;
         for (; c0 + 8 <= c; c0 += 8) proj_panel<5, 3>(V, ld, t.row0, t.row1, w, c0, ew, wsum);
         if (c0 < c) proj_panel_hybrid(V, ld, t.row0, t.row1, w, c0, c - c0, ew, wsum);
+        pdl_trigger();
         proj_combine(wsum, c, red);        // red[c] (pass 1) came from the scan
     } else {
         // 16-column panels (measured fastest for the FP64 kernel: 64
@@ -434,6 +439,7 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
             if (pass == 1) proj_panel_fp64<true>(V, ld, t.row0, t.row1, w, c0, c - c0, wsum);
             else proj_panel_fp64<false>(V, ld, t.row0, t.row1, w, c0, c - c0, wsum);
         }
+        pdl_trigger();
         proj_combine(wsum, c + (pass == 1 ? 1 : 0), red);
     }
     __syncthreads();
@@ -520,6 +526,7 @@ template <bool HY, bool ONE>
 __global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__restrict__ probs,
                                                const Tile *__restrict__ tiles, const Problem P1, int tr,
                                                int s, int pass) {
+    pdl_wait();
     const TileRows<ONE> t(tiles, P1, tr);
     const Problem &P = ONE ? P1 : probs[t.prob];
     State *S = P.st;
@@ -604,6 +611,7 @@ __global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__rest
         w[r] = acc;
         nrm = fma(acc, acc, nrm);
     }
+    pdl_trigger();
     nrm = block_sum0(nrm, scratch);
     if (threadIdx.x == 0) mine[0] = nrm;
     __syncthreads();
@@ -742,15 +750,15 @@ void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const Spmv
     if (!external_w) {
         if (fp32_any) {
             prof_begin(s);
-            k_prep<<<ntiles, TPB, 0, s>>>(P_d, tiles_d, step, 0, nullptr);
+            (void)launch_pdl(k_prep, dim3(ntiles), dim3(TPB), s, P_d, tiles_d, step, 0, (double *)nullptr);
             prof_end(KC_SPMV, s);
             prof_begin(s);
-            k_spmv_step<true><<<spmv_grid(nstiles), TPB, 0, s>>>(P_d, stiles_d, nstiles, step);
+            (void)launch_pdl(k_spmv_step<true>, dim3(spmv_grid(nstiles)), dim3(TPB), s, P_d, stiles_d, nstiles, step);
             prof_end(KC_SPMV, s);
             launch_counter() += 2;
         }
         prof_begin(s);
-        k_spmv_step<false><<<spmv_grid(nstiles), TPB, 0, s>>>(P_d, stiles_d, nstiles, step);
+        (void)launch_pdl(k_spmv_step<false>, dim3(spmv_grid(nstiles)), dim3(TPB), s, P_d, stiles_d, nstiles, step);
         prof_end(KC_SPMV, s);
         launch_counter() += 1;
     }
@@ -785,15 +793,16 @@ void launch_cgs_kernel(const Problem *P_d, const Tile *tiles_d, int ntiles, cons
     if (one) P1 = *one;
     else memset(&P1, 0, sizeof P1);
     const int code = (which << 2) | (hybrid ? 2 : 0) | (one ? 1 : 0);
+    const dim3 g(ntiles), b(TPB);
     switch (code) {
-    case 0: k_proj<false, false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
-    case 1: k_proj<false, true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
-    case 2: k_proj<true, false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
-    case 3: k_proj<true, true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
-    case 4: k_apply<false, false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
-    case 5: k_apply<false, true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
-    case 6: k_apply<true, false><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
-    default: k_apply<true, true><<<ntiles, TPB, 0, s>>>(P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 0: (void)launch_pdl(k_proj<false, false>, g, b, s, P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 1: (void)launch_pdl(k_proj<false, true>, g, b, s, P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 2: (void)launch_pdl(k_proj<true, false>, g, b, s, P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 3: (void)launch_pdl(k_proj<true, true>, g, b, s, P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 4: (void)launch_pdl(k_apply<false, false>, g, b, s, P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 5: (void)launch_pdl(k_apply<false, true>, g, b, s, P_d, tiles_d, P1, one_tr, step, pass); break;
+    case 6: (void)launch_pdl(k_apply<true, false>, g, b, s, P_d, tiles_d, P1, one_tr, step, pass); break;
+    default: (void)launch_pdl(k_apply<true, true>, g, b, s, P_d, tiles_d, P1, one_tr, step, pass); break;
     }
     launch_counter() += 1;
 }
