@@ -1,9 +1,12 @@
 // diag.cu -- throughput probes used to state roofline denominators.
 //
 // hlanc_diag_fp64_tflops: dense FP64 FMA throughput of the device (eight
-// independent FMA chains per thread, 8 CTAs of 256 threads per SM).  The
-// CGS kernels issue one FP64 FMA per 8-byte element, so on GB300 their
-// ceiling is min(HBM bandwidth, this rate x 8 bytes / 2 flops).
+// independent FMA chains per thread, 8 CTAs of 256 threads per SM).  An
+// all-FP64 CGS kernel issues one FP64 FMA per 8-byte element, so on GB300
+// its ceiling is min(HBM bandwidth, this rate x 8 bytes / 2 flops); the
+// hybrid kernels put part of the columns on the integer pipes to pass it.
+// (hlanc_diag_cgs, the CGS kernels alone, lives in engine.cu beside the
+// engine it sets up.)
 #include <cuda_runtime.h>
 
 #include "internal.cuh"

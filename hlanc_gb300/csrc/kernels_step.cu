@@ -9,10 +9,12 @@
 // the device by the last CTA of each kernel, so a whole restart cycle runs
 // without host synchronisation and can be captured in one CUDA graph.
 //
-// GB300 note: these kernels stream V once per pass with one FP64 FMA per
-// element.  Blackwell Ultra's FP64 rate is low, so each inner loop issues
-// exactly one DFMA per loaded element and every reduction is accumulated in
-// registers over a whole tile before the (few) shuffle additions.
+// GB300 note: these kernels stream V once per pass.  Blackwell Ultra's FP64
+// rate is low, so the CGS kernels issue at most one DFMA per loaded element,
+// run part of every column panel as exact fixed-point integer products on
+// the integer pipes (fixed_point.cuh; launches over >= 2^18 rows), and
+// accumulate every reduction in registers over a whole tile before the
+// (few) shuffle additions.
 #include <float.h>
 #include <string.h>
 
@@ -234,10 +236,10 @@ __global__ void __launch_bounds__(TPB) k_prep(const Problem *__restrict__ probs,
 }
 
 // ---- CGS projection: h = V[:, 0:c)^T w  (+ ||w||^2 on pass 1) ----------------
-// Thread per row, columns in panels of at most 8: each thread keeps one
-// accumulator per panel column for all the rows it visits in the tile
-// (coalesced column reads), then one transposed warp reduction and a
-// cross-warp sum in shared memory.  Panel shapes are template parameters
+// Thread per row, columns in panels (16 wide for the FP64 kernel, 8 for the
+// hybrid one): each thread keeps one accumulator per panel column for all
+// the rows it visits in the tile (coalesced column reads), then one
+// transposed warp reduction per panel.  Panel shapes are template parameters
 // picked from the device-known column count, so no instruction is issued
 // for an absent column (predicated-off FP64 instructions still occupy
 // GB300's FP64 pipe).

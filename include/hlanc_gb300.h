@@ -263,7 +263,8 @@ typedef struct {
 int hlanc_last_profile(hlanc_profile_t *out);
 
 /* Measured dense FP64 FMA throughput of device `dev` (TFLOP/s): the ceiling
- * of kernels that issue one FP64 FMA per loaded 8-byte element. */
+ * of kernels that issue one FP64 FMA per loaded 8-byte element (the
+ * all-FP64 CGS kernels). */
 int hlanc_diag_fp64_tflops(int dev, double *tflops);
 /* The CGS kernels alone on a synthetic basis of n rows and c columns
  * (cgs_kernel HLANC_CGS_FP64 or HLANC_CGS_HYBRID), each launched reps times

@@ -50,6 +50,18 @@ def test_struct_layouts_match(H, tmp_path):
                                      C.sizeof(H.ServerOpts), H.Opts.profile.offset]
 
 
+def test_cgs_diag_rejects_bad_arguments(H):
+    # argument checks come before any CUDA call
+    ms = (C.c_double * 3)()
+    f = H.lib().hlanc_diag_cgs
+    bad = 2                                                         # HLANC_ERR_INVALID
+    assert f(0, 100, 8, H.HLANC_CGS_HYBRID, 1, ms) == bad         # n < 1024
+    assert f(0, 4096, 1, H.HLANC_CGS_HYBRID, 1, ms) == bad        # c < 2
+    assert f(0, 4096, 8, H.HLANC_CGS_AUTO, 1, ms) == bad          # mode must be FP64 or HYBRID
+    assert f(0, 4096, H.HLANC_MAX_NCV + 1, H.HLANC_CGS_FP64, 1, ms) == bad
+    assert f(0, 4096, 8, H.HLANC_CGS_FP64, 1, None) == bad
+
+
 def test_status_strings(H):
     assert H.lib().hlanc_status_string(0) == b"ok"
     assert H.lib().hlanc_status_string(1) == b"not converged"

@@ -328,6 +328,16 @@ def test_hybrid_cgs_default_on_large_problem(H):
     _check_pairs(m, v1, x1, 8)
 
 
+def test_cgs_kernels_alone(H):
+    # hlanc_diag_cgs: both CGS kernels run on a synthetic basis and report
+    # positive times; the hybrid one is not slower than FP64 at this size
+    fp = H.cgs_kernel_ms(1 << 20, 24, H.HLANC_CGS_FP64, reps=3)
+    hy = H.cgs_kernel_ms(1 << 20, 24, H.HLANC_CGS_HYBRID, reps=3)
+    for r in (fp, hy):
+        assert all(0.0 < v < 1000.0 for v in r.values()), r
+    assert hy["proj"] <= 1.1 * fp["proj"]
+
+
 def test_native_library_loaded(H):
     import os
     with open("/proc/self/maps") as f:
