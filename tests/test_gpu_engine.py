@@ -93,6 +93,26 @@ def test_batch_matches_solo(H, torch):
         assert np.linalg.norm(R, axis=0).max() <= 1e-10 * _norm_a(m)
 
 
+def test_batch_hybrid_cgs_matches_solo(H, torch):
+    # forced hybrid CGS in a batched launch (descriptors from the launch
+    # tables, one tile table over all problems) against FP64 solo solves
+    mats = _batch_mats(8, seed=11)
+    ops = [H.dcsrmv_operator_gpu(m) for m in mats]
+    b = H.Batch(ops, 4, 12, cgs=H.HLANC_CGS_HYBRID)
+    vals = [torch.zeros(12, dtype=torch.float64, device="cuda") for _ in mats]
+    vecs = [torch.zeros((12, m.n), dtype=torch.float64, device="cuda") for m in mats]
+    status, st = b.run([v.data_ptr() for v in vals], [x.data_ptr() for x in vecs])
+    assert np.all(status == 0), status
+    for m, op, v, x in zip(mats, ops, vals, vecs):
+        rc, sv, _, _ = H.solve(op, 4, 12, cgs=H.HLANC_CGS_FP64)
+        assert rc == 0
+        got = v.cpu().numpy()[:4]
+        assert np.abs(got - sv[:4]).max() <= 1e-10 * np.abs(sv[:4]).max()
+        X = x.cpu().numpy()[:4].T
+        R = G.to_scipy(m) @ X - X * got
+        assert np.linalg.norm(R, axis=0).max() <= 1e-10 * _norm_a(m)
+
+
 def test_batch_mixed_precision(H, torch):
     mats = _batch_mats(6, seed=5)
     ops = [H.dcsrmv_operator_gpu(m, precision=H.HLANC_PREC_FP32_REFINE) for m in mats]

@@ -328,6 +328,36 @@ def test_hybrid_cgs_default_on_large_problem(H):
     _check_pairs(m, v1, x1, 8)
 
 
+def test_hybrid_cgs_host_operator_and_mixed_precision(H):
+    # forced hybrid CGS where w arrives from a host callback, and in the
+    # FP32 phase + FP64 refinement of a mixed-precision solve (the shifted
+    # 3-D Laplacian has simple eigenvalues; single-vector Lanczos returns
+    # one copy of a multiple one)
+    m = G.laplacian_3d(10, shift_seed=1)
+    A = G.to_scipy(m)
+
+    def op(x, y):
+        y[:] = A @ x
+
+    o = H.opts(cgs=H.HLANC_CGS_HYBRID, tol=1e-10)        # (opts, buffers it keeps alive)
+    values = np.zeros(16)
+    vectors = np.zeros((m.n, 16), order="F")
+    rc = H.ds_solver_gpu(m.n, 4, 16, values, vectors, m.n, op, opts_=o)
+    assert rc == 0
+    ref = np.sort(np.linalg.eigvalsh(A.toarray()))[-4:]
+    assert np.abs(values[:4] - ref).max() <= EV_RTOL * np.abs(ref).max()
+    _check_pairs(m, values, vectors, 4)
+
+    g = golden("chunglu_4096.npz")
+    m2 = G.chung_lu_normalized(4096, seed=2)
+    op2 = H.dcsrmv_operator_gpu(m2, precision=H.HLANC_PREC_FP32_REFINE)
+    rc, vals, vecs, st = H.solve(op2, 16, 48, precision=H.HLANC_PREC_FP32_REFINE, seed=int(g["seed"]),
+                                 cgs=H.HLANC_CGS_HYBRID)
+    assert rc == 0, st
+    assert np.abs(vals[:16] - g["values"]).max() <= EV_RTOL * np.abs(g["values"]).max()
+    _check_pairs(m2, vals, vecs, 16)
+
+
 def test_cgs_kernels_alone(H):
     # hlanc_diag_cgs: both CGS kernels run on a synthetic basis and report
     # positive times; the hybrid one is not slower than FP64 at this size
