@@ -169,7 +169,8 @@ __device__ __forceinline__ void spmv_unit(const SpmvTile &t, const int *__restri
 
 // ---- SpMV of the step --------------------------------------------------------
 // One CTA per SpMV unit (the hardware scheduler balances skewed units).
-// v_j -> V[:, j] for the unit's rows, w = A v_j (FP64: A r, one scaling per row).
+// v_j -> V[:, j] for the unit's rows, w = A v_j (FP64: A r, one scaling per row;
+// in the FP32 form k_prep wrote V[:, j] and its FP32 copy beforehand).
 // Six resident CTAs per SM (40 registers) keep enough gathers in flight: on
 // GB300 this measured 18% faster than the unbounded 72-register build on the
 // 4.1M-row Laplacian (70% of HBM standalone) and 14% faster on the power-law
@@ -195,17 +196,17 @@ __global__ void __launch_bounds__(TPB, SPMV_CTAS_PER_SM) k_spmv_step(const Probl
     const double *__restrict__ rin = step_in(P, j);
     double *__restrict__ w = step_out(P, j);
     double *__restrict__ vj = P.V + (size_t)j * P.ld;
-    if (!F32)
-        for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
-            const double x = rin[r];
-            vj[r] = scale ? x * t1 : x;
-        }
     if constexpr (F32) {
         spmv_unit<float>(t, P.row_ptr, P.col, P.val32, P.x32, s_col, s_val, red,
                          [=](int rr, float acc) { w[rr] = (double)acc; });
     } else {
-        spmv_unit<double>(t, P.row_ptr, P.col, P.val, rin, s_col, s_val, red,
-                          [=](int rr, double acc) { w[rr] = scale ? acc * t1 : acc; });
+        // each row is emitted once: V[:, j] is written there too, instead of
+        // in a separate pass over the unit's rows before the gathers start
+        spmv_unit<double>(t, P.row_ptr, P.col, P.val, rin, s_col, s_val, red, [=](int rr, double acc) {
+            const double x = rin[rr];
+            w[rr] = scale ? acc * t1 : acc;
+            vj[rr] = scale ? x * t1 : x;
+        });
     }
     pdl_trigger();
 }
