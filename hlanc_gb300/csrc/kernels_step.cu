@@ -175,10 +175,12 @@ __device__ __forceinline__ void spmv_unit(const SpmvTile &t, const int *__restri
 // GB300 this measured 18% faster than the unbounded 72-register build on the
 // 4.1M-row Laplacian (70% of HBM standalone) and 14% faster on the power-law
 // graph; streaming (evict-first) loads of the entries were slower, because
-// neighbouring rows share their cache sectors.
+// neighbouring rows share their cache sectors.  The FP32 step kernel runs at
+// 5 CTAs per SM: at 6 it spilled, and 5 measured 0.5% faster on the
+// mixed-precision power-law solve.
 constexpr int SPMV_CTAS_PER_SM = 6;
 template <bool F32>
-__global__ void __launch_bounds__(TPB, SPMV_CTAS_PER_SM) k_spmv_step(const Problem *__restrict__ probs,
+__global__ void __launch_bounds__(TPB, F32 ? 5 : SPMV_CTAS_PER_SM) k_spmv_step(const Problem *__restrict__ probs,
                                                    const SpmvTile *__restrict__ tiles, int ntiles, int s) {
     using T = typename std::conditional<F32, float, double>::type;
     __shared__ int s_col[(TPB / 32) * STAGE];
