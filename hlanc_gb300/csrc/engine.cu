@@ -1358,9 +1358,16 @@ int hlanc_diag_cgs(int dev, int n, int c, int cgs_kernel, int reps, double *ms3)
     S.need3 = 0;
     S.rnorm = S.wnorm = sqrt((double)n);
     CK(cudaMemcpyAsync(p.st, &S, sizeof S, cudaMemcpyHostToDevice, E.stream));
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
+    struct Events {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        ~Events() {
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+        }
+    } ev;
+    CK(cudaEventCreate(&ev.e0));
+    CK(cudaEventCreate(&ev.e1));
+    cudaEvent_t e0 = ev.e0, e1 = ev.e1;
     const bool hy = cgs_kernel == HLANC_CGS_HYBRID;
     const int pass_of[3] = {1, 2, 2}, which_of[3] = {0, 0, 1};
     for (int q = 0; q < 3; ++q) {
@@ -1375,8 +1382,6 @@ int hlanc_diag_cgs(int dev, int n, int c, int cgs_kernel, int reps, double *ms3)
         CK(cudaEventElapsedTime(&ms, e0, e1));
         ms3[q] = ms / reps;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     CK(cudaGetLastError());
     return HLANC_OK;
 }
