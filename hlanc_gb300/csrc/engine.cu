@@ -511,10 +511,12 @@ public:
     }
 
     // graph key for the basis kernel instantiation launch_basis picks
+    // Template width of the basis update for an (adjusted) nev: up to 64
+    // outputs in registers; beyond that (ncv > 64 only) the wide kernel.
     static int basis_bucket(int nev) {
         if (nev <= 0) return 0;
         const int q = (nev + 3) / 4;
-        return q <= 10 ? 4 * q : q <= 12 ? 48 : q <= 14 ? 56 : 64;
+        return q <= 10 ? 4 * q : q <= 12 ? 48 : q <= 14 ? 56 : q <= 16 ? 64 : HLANC_MAX_NCV;
     }
 
     // Device part of one cycle: apply pending restarts, extend, (restart), gather.

@@ -409,6 +409,62 @@ __global__ void __launch_bounds__(TPB) k_basis(const Problem *__restrict__ probs
     }
 }
 
+// The same update when the adjusted nev exceeds the 64 outputs k_basis and
+// k_basis_tc hold (possible for ncv > 64: nev grows by up to half of np).
+// The update is in place and every output reads every column of the row, so
+// each thread first copies its row of V to shared memory (64 threads per
+// CTA, a row of up to 128 columns each), then writes the outputs in order.
+// The sums run over k in ascending order with the same band as k_basis, so
+// the results are the same.
+constexpr int WIDE_TPB = 64;
+__global__ void __launch_bounds__(WIDE_TPB) k_basis_wide(const Problem *__restrict__ probs,
+                                                         const Tile *__restrict__ tiles) {
+    const Tile t = tiles[blockIdx.x];
+    const Problem &P = probs[t.prob];
+    State *S = P.st;
+    if (S->status != ST_RUNNING || S->phase != PH_APPLY) return;
+    const int m = P.ncv, nev = S->nev, np = S->np;
+    extern __shared__ double rows[];               // WIDE_TPB x (m + 1): each thread's row
+    const double *Q = P.small + SM_Q(m);
+    const double *h = P.small + SM_H(m);
+    __shared__ double scratch[32], mine[1], tot[1];
+    const double hn = h[nev];
+    const double qlast = Q[(m - 1) + (size_t)(nev - 1) * m];
+    const double *__restrict__ rin = (m & 1) ? P.r1 : P.r0;
+    double *__restrict__ rout = (nev & 1) ? P.r1 : P.r0;
+    const size_t ld = (size_t)P.ld;
+    double *my = rows + (size_t)threadIdx.x * (m + 1);
+    double nrm = 0.0;
+    for (int r = t.row0 + threadIdx.x; r < t.row1; r += WIDE_TPB) {
+        double *vr = P.V + r;
+        for (int k = 0; k < m; ++k) my[k] = vr[(size_t)k * ld];
+        for (int i = 0; i < nev; ++i) {
+            const int k1 = min(m, i + np + 1);     // band of output i: k <= i + np
+            const double *qi = Q + (size_t)i * m;
+            double acc = 0.0;
+            for (int k = 0; k < k1; ++k) acc = fma(my[k], qi[k], acc);
+            vr[(size_t)i * ld] = acc;
+        }
+        const double *qn = Q + (size_t)nev * m;
+        double accn = 0.0;
+        for (int k = 0; k < m; ++k) accn = fma(my[k], qn[k], accn);
+        double res = rin[r] * qlast;                // HLanc.hpp:1605-1614
+        if (hn > 0.0) res = res + hn * accn;
+        rout[r] = res;
+        nrm = fma(res, res, nrm);
+    }
+    nrm = block_sum0(nrm, scratch);
+    if (threadIdx.x == 0) mine[0] = nrm;
+    __syncthreads();
+    if (!finish_tile(P, blockIdx.x - P.tile0, 1, mine, tot)) return;
+    if (threadIdx.x == 0) {
+        S->rnorm = sqrt(tot[0]);                    // HLanc.hpp:1735
+        S->phase = PH_EXTEND;
+        S->sumnev += nev;
+        S->napply += 1;
+    }
+}
+
 // ---- finalize: converged Ritz pairs (HLanc.hpp:1765-1842) -------------------
 __global__ void __launch_bounds__(RTPB) k_finalize(const Problem *__restrict__ probs) {
     const Problem &P = probs[blockIdx.x];
@@ -668,6 +724,20 @@ void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_n
                   bool tensor_cores, cudaStream_t s) {
     if (tensor_cores && basis_tc_fits(max_ncv, max_nev)) {
         launch_basis_tc(P_d, tiles_d, ntiles, max_nev, s);
+        return;
+    }
+    if (max_nev > 64) {
+        const size_t smem = sizeof(double) * (size_t)WIDE_TPB * (max_ncv + 1);
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_basis_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(double) * WIDE_TPB * (MAXNCV + 1)));
+            attr = true;
+        }
+        prof_begin(s);
+        k_basis_wide<<<ntiles, WIDE_TPB, smem, s>>>(P_d, tiles_d);
+        prof_end(KC_BASIS, s);
+        launch_counter() += 1;
         return;
     }
     switch ((max_nev + 3) / 4) {

@@ -358,6 +358,24 @@ def test_hybrid_cgs_host_operator_and_mixed_precision(H):
     _check_pairs(m2, vals, vecs, 16)
 
 
+def test_largest_basis(H):
+    # ncv = HLANC_MAX_NCV with nev 40: the adjusted nev grows past 64 (up to
+    # half of np is added), so the restart takes the wide basis kernel; the
+    # hybrid CGS kernels carry up to 128 columns (the update's integer
+    # accumulators at their Cauchy-Schwarz bound)
+    m = G.laplacian_3d(20, shift_seed=1)
+    op = H.dcsrmv_operator_gpu(m)
+    ncv = H.HLANC_MAX_NCV
+    ref = np.sort(np.linalg.eigvalsh(G.to_scipy(m).toarray()))[-40:]
+    rc1, v1, x1, s1 = H.solve(op, 40, ncv, tol=1e-10, cgs=H.HLANC_CGS_HYBRID)
+    rc2, v2, x2, s2 = H.solve(op, 40, ncv, tol=1e-10, cgs=H.HLANC_CGS_FP64)
+    assert rc1 == rc2 == 0
+    for v, x in ((v1, x1), (v2, x2)):
+        assert np.abs(v[:40] - ref).max() <= EV_RTOL * np.abs(ref).max()
+        _check_pairs(m, v, x, 40)
+    assert np.abs(v1[:40] - v2[:40]).max() <= 1e-12 * np.abs(v2[:40]).max()
+
+
 def test_cgs_kernels_alone(H):
     # hlanc_diag_cgs: both CGS kernels run on a synthetic basis and report
     # positive times; the hybrid one is not slower than FP64 at this size
