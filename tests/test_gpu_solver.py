@@ -376,6 +376,43 @@ def test_largest_basis(H):
     assert np.abs(v1[:40] - v2[:40]).max() <= 1e-12 * np.abs(v2[:40]).max()
 
 
+def test_largest_basis_device_restart(H):
+    # the same envelope with the restart math in device kernels
+    m = G.laplacian_3d(20, shift_seed=1)
+    op = H.dcsrmv_operator_gpu(m)
+    ref = np.sort(np.linalg.eigvalsh(G.to_scipy(m).toarray()))[-40:]
+    rc, v, x, st = H.solve(op, 40, H.HLANC_MAX_NCV, tol=1e-10, restart_on_device=True)
+    assert rc == 0, st
+    assert np.abs(v[:40] - ref).max() <= EV_RTOL * np.abs(ref).max()
+    _check_pairs(m, v, x, 40)
+
+
+def test_largest_nev_tensor_core_basis(H):
+    # nev = HLANC_MAX_NEV with ncv = 64: the tensor-core basis update at its
+    # widest (nev + 1 = 64 outputs).  With np = 1 a restart adds one Lanczos
+    # step, so the spectrum is chosen to converge fast: 63 large, separated
+    # eigenvalues above a tight cluster near zero, weakly coupled.
+    n = 400
+    rng = np.random.default_rng(21)
+    d = np.concatenate([100.0 + 3.0 * np.arange(63), 1e-3 * rng.random(n - 63)])
+    d = d[rng.permutation(n)]
+    rp, ci, va = [0], [], []
+    for i in range(n):
+        for j, x in ((i - 1, 1e-3), (i, d[i]), (i + 1, 1e-3)):
+            if 0 <= j < n:
+                ci.append(j)
+                va.append(x)
+        rp.append(len(ci))
+    m = G.CSR(n, n, np.array(rp, dtype=np.int32), np.array(ci, dtype=np.int32), np.array(va))
+    op = H.dcsrmv_operator_gpu(m)
+    nev = H.HLANC_MAX_NEV
+    ref = np.sort(np.linalg.eigvalsh(G.to_scipy(m).toarray()))[-nev:]
+    rc, v, x, st = H.solve(op, nev, 64, tol=1e-10)
+    assert rc == 0, st
+    assert np.abs(v[:nev] - ref).max() <= EV_RTOL * np.abs(ref).max()
+    _check_pairs(m, v, x, nev)
+
+
 def test_cgs_kernels_alone(H):
     # hlanc_diag_cgs: both CGS kernels run on a synthetic basis and report
     # positive times; the hybrid one is not slower than FP64 at this size
