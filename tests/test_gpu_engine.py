@@ -113,6 +113,28 @@ def test_batch_hybrid_cgs_matches_solo(H, torch):
         assert np.linalg.norm(R, axis=0).max() <= 1e-10 * _norm_a(m)
 
 
+def test_batch_mixed_basis_widths(H, torch):
+    # one problem with ncv = 100 (its adjusted nev passes 64, so the whole
+    # launch takes the wide basis kernel) batched with small ones; each
+    # problem keeps its own nev inside that kernel
+    mats = [G.laplacian_3d(12, shift_seed=1)] + _batch_mats(2, seed=13)
+    nevs = [30, 4, 4]
+    ncvs = [100, 12, 12]
+    ops = [H.dcsrmv_operator_gpu(m) for m in mats]
+    b = H.Batch(ops, nevs, ncvs, tol=1e-10)
+    vals = [torch.zeros(c, dtype=torch.float64, device="cuda") for c in ncvs]
+    vecs = [torch.zeros((c, m.n), dtype=torch.float64, device="cuda") for c, m in zip(ncvs, mats)]
+    status, st = b.run([v.data_ptr() for v in vals], [x.data_ptr() for x in vecs])
+    assert np.all(status == 0), status
+    for m, op, v, x, k, c in zip(mats, ops, vals, vecs, nevs, ncvs):
+        ref = np.sort(np.linalg.eigvalsh(G.to_scipy(m).toarray()))[-k:]
+        got = v.cpu().numpy()[:k]
+        assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max()
+        X = x.cpu().numpy()[:k].T
+        R = G.to_scipy(m) @ X - X * got
+        assert np.linalg.norm(R, axis=0).max() <= 1e-10 * _norm_a(m)
+
+
 def test_batch_mixed_precision(H, torch):
     mats = _batch_mats(6, seed=5)
     ops = [H.dcsrmv_operator_gpu(m, precision=H.HLANC_PREC_FP32_REFINE) for m in mats]
