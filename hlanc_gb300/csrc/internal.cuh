@@ -226,6 +226,19 @@ __device__ __forceinline__ double block_sum0(double v, double *scratch /* >= 32 
     return s;
 }
 
+// Raise a kernel's dynamic shared-memory limit.  The attribute belongs to
+// the current device, so it is set once per device (a bit per device in
+// `done`, per call site); devices past 63 set it on every call.
+template <typename K>
+inline void smem_limit_once(K *kernel, int bytes, std::atomic<unsigned long long> &done) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return;
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    done.fetch_or(bit, std::memory_order_release);
+}
+
 // ---- programmatic dependent launch between the kernels of a Lanczos step --
 // Every step kernel waits for its predecessor at entry (griddepcontrol.wait
 // returns once the previous grid has completed and its writes are visible;

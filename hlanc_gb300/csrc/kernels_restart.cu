@@ -708,11 +708,8 @@ void launch_restart(const Problem *P_d, int nprob, int, cudaStream_t s) {
 template <int MAXOUT>
 static void basis_t(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, cudaStream_t s) {
     const size_t smem = sizeof(double) * (size_t)max_ncv * (MAXOUT + 1);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_basis<MAXOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    smem_limit_once(k_basis<MAXOUT>, 160 * 1024, attr);
     prof_begin(s);
     k_basis<MAXOUT><<<ntiles, TPB, smem, s>>>(P_d, tiles_d);
     prof_end(KC_BASIS, s);
@@ -728,12 +725,8 @@ void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_n
     }
     if (max_nev > 64) {
         const size_t smem = sizeof(double) * (size_t)WIDE_TPB * (max_ncv + 1);
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(k_basis_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(double) * WIDE_TPB * (MAXNCV + 1)));
-            attr = true;
-        }
+        static std::atomic<unsigned long long> attr{0};
+        smem_limit_once(k_basis_wide, (int)(sizeof(double) * WIDE_TPB * (MAXNCV + 1)), attr);
         prof_begin(s);
         k_basis_wide<<<ntiles, WIDE_TPB, smem, s>>>(P_d, tiles_d);
         prof_end(KC_BASIS, s);
@@ -767,11 +760,8 @@ void launch_finalize(const Problem *P_d, int nprob, int, cudaStream_t s) {
 
 void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, cudaStream_t s) {
     const size_t smem = sizeof(double) * (size_t)max_ncv * RITZ_PANEL;
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_ritz, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    smem_limit_once(k_ritz, 64 * 1024, attr);
     prof_begin(s);
     k_ritz<<<ntiles, TPB, smem, s>>>(P_d, tiles_d);
     prof_end(KC_RITZ, s);

@@ -470,12 +470,9 @@ static size_t basis_tc_smem() {
 
 template <int NPAD>
 static void basis_tc_t(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s) {
-    static bool attr = false;
+    static std::atomic<unsigned long long> attr{0};
     const size_t smem = basis_tc_smem<NPAD>();
-    if (!attr) {
-        cudaFuncSetAttribute(k_basis_tc<NPAD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = true;
-    }
+    smem_limit_once(k_basis_tc<NPAD>, (int)smem, attr);
     prof_begin(s);
     k_basis_tc<NPAD><<<ntiles, tc::THREADS, smem, s>>>(P_d, tiles_d);
     prof_end(KC_BASIS, s);
