@@ -511,12 +511,14 @@ public:
     }
 
     // graph key for the basis kernel instantiation launch_basis picks
-    // Template width of the basis update for an (adjusted) nev: up to 64
-    // outputs in registers; beyond that (ncv > 64 only) the wide kernel.
+    // Width class of the basis update for an (adjusted) nev: the tensor-core
+    // kernel takes nev + 1 <= 64 outputs (nev <= 63, bucket 63), the FP64
+    // kernel up to 64 outputs in registers, and the wide kernel the rest
+    // (ncv > 64 only).
     static int basis_bucket(int nev) {
         if (nev <= 0) return 0;
         const int q = (nev + 3) / 4;
-        return q <= 10 ? 4 * q : q <= 12 ? 48 : q <= 14 ? 56 : q <= 16 ? 64 : HLANC_MAX_NCV;
+        return q <= 10 ? 4 * q : q <= 12 ? 48 : q <= 14 ? 56 : nev <= 63 ? 63 : nev == 64 ? 64 : HLANC_MAX_NCV;
     }
 
     // Device part of one cycle: apply pending restarts, extend, (restart), gather.

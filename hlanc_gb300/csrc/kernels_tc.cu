@@ -480,8 +480,8 @@ static void basis_tc_t(const Problem *P_d, const Tile *tiles_d, int ntiles, cuda
 }
 
 // The tensor-core basis update serves problems with ncv <= 64 and
-// nev + 1 <= 64 (nev_max is the engine's bucket of nev, so nev <= 60 in
-// practice); the caller uses k_basis otherwise.
+// nev + 1 <= 64 (nev_max is the engine's bucket of the adjusted nev: 4, 8,
+// ..., 40, 48, 56 or 63); the caller uses k_basis otherwise.
 bool basis_tc_fits(int max_ncv, int nev_max) { return max_ncv <= tc::KMAX && nev_max + 1 <= tc::NMAX; }
 
 void launch_basis_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, int nev_max, cudaStream_t s) {

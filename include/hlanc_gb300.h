@@ -39,7 +39,7 @@ extern "C" {
 
 /* Kernel of the restart's basis update V <- V Q (hlanc_opts_t.basis_kernel). */
 #define HLANC_BASIS_AUTO          0  /* tensor cores (FP64-accurate integer splitting) when
-                                        ncv <= 64 and nev <= 60, else the FP64 kernel */
+                                        ncv <= 64 (so nev <= 63), else the FP64 kernel */
 #define HLANC_BASIS_FP64          1  /* always the FP64 CUDA-core kernel */
 
 /* Arithmetic of the CGS passes h = V^T w, w -= V h (hlanc_opts_t.cgs_kernel).
