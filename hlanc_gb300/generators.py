@@ -223,6 +223,26 @@ def batched_problem_sizes(count: int = 512, n_lo: int = 2000, n_hi: int = 200000
     return n, bw
 
 
+def _count_le(cdf: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """searchsorted(cdf, uniform01 of the raw draws x, side="right") for a
+    sorted cdf in [0, 1], through a bucket index: bucket b = x >> (64 - k)
+    holds the draws in [b 2^-k, (b+1) 2^-k), lo[b] counts the cdf entries
+    below the bucket, and the few entries inside it are compared directly.
+    Exactly the same counts as the binary search, several times fewer
+    random memory accesses."""
+    k = max(10, min(26, int(np.ceil(np.log2(max(cdf.size, 2)))) + 2))
+    edges = np.arange((1 << k) + 1, dtype=np.float64) * (2.0 ** -k)
+    lo = np.searchsorted(cdf, edges, side="right")
+    span = int(np.diff(lo).max()) if lo.size > 1 else 0
+    u = (x >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+    base = lo[(x >> np.uint64(64 - k)).astype(np.int64)]
+    padded = np.concatenate([cdf, np.full(span + 1, np.inf)])
+    out = base.copy()
+    for t in range(span):
+        out += padded[base + t] <= u
+    return out
+
+
 def chung_lu_normalized(n: int, gamma: float = 2.5, mean_degree: float = 32.0, seed: int = 2) -> CSR:
     """Symmetric normalised adjacency D^-1/2 A D^-1/2 of a Chung-Lu graph.
 
@@ -246,25 +266,30 @@ def chung_lu_normalized(n: int, gamma: float = 2.5, mean_degree: float = 32.0, s
         w = (i + i0) ** (-expo)
         return w * (mean_degree * n / w.sum())
 
+    def first_weight(i0):            # weights(i0)[0] without scaling the whole array
+        w = (i + i0) ** (-expo)
+        return w[0] * (mean_degree * n / w.sum())
+
     lo, hi = 1e-3, float(n)
     for _ in range(100):     # bisection on i0 so that w_0 = target
         mid = np.sqrt(lo * hi)
-        if weights(mid)[0] > target:
-            lo = mid
-        else:
-            hi = mid
+        nlo, nhi = (mid, hi) if first_weight(mid) > target else (lo, mid)
+        if nlo == lo and nhi == hi:  # fixed point: the remaining steps change nothing
+            break
+        lo, hi = nlo, nhi
     w = weights(hi)
     cdf = np.cumsum(w)
     cdf /= cdf[-1]
     m = int(round(n * mean_degree / 2))
-    ua = uniform01(seed, STREAM_GRAPH, m)
-    ub = uniform01(seed, STREAM_GRAPH, m, offset=m)
-    a = np.minimum(np.searchsorted(cdf, ua, side="right"), n - 1)
-    b = np.minimum(np.searchsorted(cdf, ub, side="right"), n - 1)
+    ua = u64(seed, STREAM_GRAPH, m)
+    ub = u64(seed, STREAM_GRAPH, m, offset=m)
+    a = np.minimum(_count_le(cdf, ua), n - 1)
+    b = np.minimum(_count_le(cdf, ub), n - 1)
     keep = a != b
     a, b = a[keep], b[keep]
-    adj = coo_matrix((np.ones(a.size), (a, b)), shape=(n, n)).tocsr()
-    adj = adj + adj.T
+    # both orientations in one conversion (duplicates summed, then unit weights)
+    adj = coo_matrix((np.ones(2 * a.size), (np.concatenate([a, b]), np.concatenate([b, a]))),
+                     shape=(n, n)).tocsr()
     adj.data[:] = 1.0
     ncomp, labels = connected_components(adj, directed=False)
     if ncomp > 1:

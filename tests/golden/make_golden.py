@@ -4,7 +4,9 @@ oracle/build_ref.sh into oracle/_ref/libhlanc_ref.so).
 
 Run in a container where the reference sources are mounted:
 
-    ./oracle/build_ref.sh && python tests/golden/make_golden.py [reference_dir]
+    ./oracle/build_ref.sh && python tests/golden/make_golden.py REFERENCE_DIR
+    python tests/golden/make_golden.py --large   # 2^18-row cases (about a minute)
+    python tests/golden/make_golden.py --full    # full-size C2/C3 eigenvalues (tens of minutes)
 
 Every solve starts from the generators' seeded start vector (the MKL shim
 injects it where the reference calls dlarnv), so the fixtures, the oracle and
@@ -16,6 +18,7 @@ from __future__ import annotations
 
 import os
 import sys
+import time
 
 import numpy as np
 
@@ -29,20 +32,33 @@ from hlanc_gb300 import generators as G  # noqa: E402
 READERS = os.path.join(HERE, "readers")
 
 
+def fingerprint(rp, ci, v):
+    """Structure and value checksums of a CSR matrix: a test regenerates the
+    matrix from its generator and compares these before it compares
+    eigenvalues, so a generator change cannot pass as a solver change."""
+    rp, ci, v = np.asarray(rp, np.int64), np.asarray(ci, np.int64), np.asarray(v, np.float64)
+    w = np.arange(1, ci.size + 1, dtype=np.float64)
+    return np.array([rp.size - 1, ci.size, float(ci.sum()), float((ci * (np.arange(ci.size) % 7)).sum()),
+                     float(v.sum()), float(np.abs(v).sum()), float((v * w).sum() / ci.size)])
+
+
 def solve_case(name, m, nev, ncv, symmetric=False, seed=0, keep_vectors=False, **extra):
     x0 = G.start_vector(m.n if hasattr(m, "n") else len(m["row_ptr"]) - 1, seed)
     if isinstance(m, dict):
         rp, ci, v, nc = m["row_ptr"], m["col"], m["val"], m["ncols"]
     else:
         rp, ci, v, nc = m.row_ptr, m.col, m.val, m.ncols
+    t0 = time.perf_counter()
     rc, vals, vecs, calls = O.ref_solve_csr(rp, ci, v, nc, symmetric, nev, ncv, x0)
+    dt = time.perf_counter() - t0
     assert rc == 0, (name, rc)
-    out = dict(values=vals[:nev], nev=nev, ncv=ncv, seed=seed, spmv_calls=calls, symmetric=symmetric)
+    out = dict(values=vals[:nev], nev=nev, ncv=ncv, seed=seed, spmv_calls=calls, symmetric=symmetric,
+               fingerprint=fingerprint(rp, ci, v), ref_seconds=dt, ref_threads=os.cpu_count() or 1)
     if keep_vectors:
         out["vectors"] = np.ascontiguousarray(vecs[:, :nev])
     out.update(extra)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
-    print(f"{name}: rc={rc} spmv={calls} top={vals[nev - 1]:.15g}")
+    print(f"{name}: rc={rc} spmv={calls} top={vals[nev - 1]:.15g} ({dt:.1f} s)", flush=True)
 
 
 def write_reader_inputs():
@@ -121,10 +137,36 @@ def spmv_fixture(readers):
     print("spmv.npz")
 
 
+def large_cases():
+    """Sizes where the library's default kernels differ from the small cases:
+    launches over >= 2^18 rows take the hybrid (FP64 + fixed-point) CGS
+    kernels and the tensor-core basis update.  About a minute on 8 cores."""
+    solve_case("lap3d_64_shift", G.laplacian_3d(64, shift_seed=1), 20, 60)
+    solve_case("chunglu_2e18", G.chung_lu_normalized(1 << 18, seed=2), 16, 48)
+
+
+def full_cases():
+    """Eigenvalues of the two single-solve workloads at full size (3-D
+    Laplacian 160^3 + shift, nev 20, ncv 60; Chung-Lu n = 2^22, nev 16,
+    ncv 48).  Tens of minutes on 8 cores; values only."""
+    solve_case("c3_chunglu_2e22", G.chung_lu_normalized(1 << 22, seed=2), 16, 48)
+    solve_case("c2_lap3d_160_shift", G.laplacian_3d(160, shift_seed=1), 20, 60)
+
+
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    flags = {a for a in sys.argv[1:] if a.startswith("--")}
+    ref_dir = args[0] if args else os.environ.get("HLANC_REFERENCE")
     if not O.ref_available():
         sys.exit("oracle/_ref/libhlanc_ref.so missing: run oracle/build_ref.sh first")
+    if "--large" in flags:
+        large_cases()
+        return
+    if "--full" in flags:
+        full_cases()
+        return
+    if not ref_dir:
+        sys.exit("usage: make_golden.py REFERENCE_DIR | --large | --full (or set HLANC_REFERENCE)")
     readers = reader_fixtures(ref_dir)
     spmv_fixture(readers)
     # the demo's cases (demo/HLanc_demo.cu): nev=4, ncv=12

@@ -153,3 +153,40 @@ def test_oracle_rejects_bad_sizes(oracle_mod):
     for nev, ncv in ((4, 4), (3, 17), (0, 5)):
         rc, *_ = oracle_mod.solve_csr(m.row_ptr, m.col, m.val, m.ncols, False, nev, ncv, x0)
         assert rc == 1
+
+
+@pytest.mark.parametrize("case,nev,ncv,gen", [
+    ("lap3d_64_shift", 20, 60, lambda: G.laplacian_3d(64, shift_seed=1)),
+    ("chunglu_2e18", 16, 48, lambda: G.chung_lu_normalized(1 << 18, seed=2)),
+])
+def test_oracle_matches_reference_at_large_n(oracle_mod, case, nev, ncv, gen):
+    """The 2^18-row fixtures that pin the GPU's default large-n kernels pin
+    the oracle too (all host threads; tens of seconds)."""
+    g = golden(f"{case}.npz")
+    m = gen()
+    rc, vals, _, st = _solve(oracle_mod, m, nev, ncv, seed=int(g["seed"]), threads=os.cpu_count() or 1)
+    assert rc == 0
+    ref = g["values"]
+    assert np.abs(vals[:nev] - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("case,gen", [
+    ("lap3d_64_shift", lambda: G.laplacian_3d(64, shift_seed=1)),
+    ("chunglu_2e18", lambda: G.chung_lu_normalized(1 << 18, seed=2)),
+    ("c2_lap3d_160_shift", lambda: G.laplacian_3d(160, shift_seed=1)),
+])
+def test_generators_reproduce_fixture_matrices(case, gen):
+    """The seeded generators rebuild the matrices the reference solved
+    (structure exactly, values to 1e-12 of their checksums)."""
+    path = os.path.join(GOLDEN, f"{case}.npz")
+    if not os.path.exists(path):
+        pytest.skip(f"{case}.npz not generated")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    m = gen()
+    fp = mg.fingerprint(m.row_ptr, m.col, m.val)
+    ref = golden(f"{case}.npz")["fingerprint"]
+    assert fp[:4].tolist() == ref[:4].tolist()
+    assert np.allclose(fp[4:], ref[4:], rtol=1e-12, atol=0)
