@@ -17,12 +17,24 @@ returned pair has ||A v - lambda v|| <= 1e-10 ||A||_inf.
     roofline  the dominant kernel class of one profiled solve (CUDA events
             around every launch): algorithmic bytes / time vs the measured
             HBM peak, and FP64 flops / time vs the live FP64 probe
+    parity  eigenvalues against the reference's own CPU solver on the same
+            matrix and start vector (tests/golden fixture), when one exists
+    forms   (default run, one GPU) the other workloads, after the timed
+            solves: the Chung-Lu graph n = 2^22 in FP64 and in mixed
+            precision (per-pair error against the reference), 512 banded
+            problems batched (FP64 and mixed) against the plain FP64 solver
+            one at a time, and a slice of the Poisson serving stream against
+            the plain FP64 solver serving one request at a time (p50/p95/p99);
+            their matrices are generated in spawned processes meanwhile
 
 `--impl reference` times the oracle's C restatement of the reference CPU
 solver (oracle/, OpenMP over all host cores) on the same workload: each step
-is one restart cycle's worth of Lanczos steps, extrapolated to the SpMV
-count of the full solve.  Multi-GPU runs are independent replicas (the
-reference path does not shard a solve): value sums every rank's rate.
+runs the first two restart cycles of the same solve and extrapolates the
+remaining Lanczos steps at the second (steady-state) cycle's cost per step,
+to the operator-application count of the reference's own full CPU solve
+(tests/golden).  `--calibrate-cpu` runs one full oracle solve to check that
+extrapolation.  Multi-GPU runs are independent replicas (the reference path
+does not shard a solve): value sums every rank's rate.
 """
 from __future__ import annotations
 
@@ -42,26 +54,20 @@ sys.path.insert(0, ROOT)
 
 from hlanc_gb300 import generators as G  # noqa: E402
 
-# SpMV calls of a full solve of each workload, measured with this library on
-# GB300 (the algorithm's count; the CPU baseline extrapolates its sampled
-# per-step time with it).
-WORKLOADS = {
-    "lap3d_160": dict(desc="3-D Laplacian 160^3 + U[0,0.1) diagonal shift (seed 1)",
-                      gen=lambda: G.laplacian_3d(160, shift_seed=1), nev=20, ncv=60, tol=1e-10),
-    "lap3d_100": dict(desc="3-D Laplacian 100^3 + U[0,0.1) diagonal shift (seed 1)",
-                      gen=lambda: G.laplacian_3d(100, shift_seed=1), nev=20, ncv=60, tol=1e-10),
-    "lap3d_64": dict(desc="3-D Laplacian 64^3 + U[0,0.1) diagonal shift (seed 1)",
-                     gen=lambda: G.laplacian_3d(64, shift_seed=1), nev=20, ncv=60, tol=1e-10),
-    "lap2d_100": dict(desc="2-D Laplacian 100^2 (reference tolerance dlamch('E'))",
-                      gen=lambda: G.laplacian_2d(100), nev=10, ncv=30, tol=0.0),
-    "chunglu_22": dict(desc="normalised adjacency of a Chung-Lu graph, n = 2^22, exponent 2.5, mean degree 32 "
-                            "(seed 2); FP32 SpMV + FP64 refinement",
-                       gen=lambda: G.chung_lu_normalized(1 << 22, seed=2), nev=16, ncv=48, tol=1e-10, mixed=True),
-    "chunglu_22_fp64": dict(desc="normalised adjacency of a Chung-Lu graph, n = 2^22 (seed 2); plain FP64",
-                            gen=lambda: G.chung_lu_normalized(1 << 22, seed=2), nev=16, ncv=48, tol=1e-10),
-}
-FULL_SOLVE_SPMV = {"lap3d_160": 3460, "lap3d_100": None, "lap3d_64": 1312, "lap2d_100": 1375,
-                   "chunglu_22": None, "chunglu_22_fp64": None}
+# Reference fixture of each workload (tests/golden/<name>.npz, written from
+# the reference's own CPU solver): eigenvalues for the parity check and the
+# operator-application count of its full solve (the CPU extrapolation).
+GOLDEN_OF = {"lap3d_160": "c2_lap3d_160_shift", "lap3d_64": "lap3d_64_shift", "lap2d_100": "c1_laplacian2d_100",
+             "chunglu_22": "c3_chunglu_2e22", "chunglu_22_fp64": "c3_chunglu_2e22"}
+
+
+def golden_of(workload):
+    name = GOLDEN_OF.get(workload)
+    path = os.path.join(ROOT, "tests", "golden", f"{name}.npz") if name else None
+    if not path or not os.path.exists(path):
+        return None
+    with np.load(path) as g:
+        return {k: g[k] for k in g.files}
 
 
 def _env_int(k, d):
@@ -201,21 +207,33 @@ def replica_value(world: int, nev: int, max_ms: float) -> float:
     return world * nev / (max_ms / 1e3)
 
 
-def cpu_sample(m, wl, threads, full_spmv):
-    """Oracle port, first restart cycle of the same solve; extrapolated."""
+def cpu_sample(m, wl, threads, full_spmv, full_src):
+    """Oracle port: the first two restart cycles of the same solve; the
+    remaining Lanczos steps are extrapolated at the second cycle's cost per
+    step (its basis widths are those of the steady state)."""
     import oracle
     oracle.build()
     x0 = G.start_vector(m.n, 0)
     t = time.perf_counter()
     rc, vals, vecs, st = oracle.solve_csr(m.row_ptr, m.col, m.val, m.ncols, False, wl["nev"], wl["ncv"], x0,
-                                          tol=wl["tol"], max_iter=1, threads=threads)
+                                          tol=wl["tol"], max_iter=2, threads=threads)
     dt = time.perf_counter() - t
-    per_spmv = dt / max(st["spmv_calls"], 1)
-    est = per_spmv * full_spmv
+    per_step = st["cycle_seconds"] / max(st["cycle_spmv"], 1)
+    est = dt + max(full_spmv - st["spmv_calls"], 0) * per_step
     return dict(value=wl["nev"] / est, unit="eigenpairs/s", cores=threads, kind="port",
-                sample=(f"first restart cycle ({st['spmv_calls']} Lanczos steps, {dt:.2f} s) of the same solve "
-                        f"on {threads} threads, extrapolated to the full solve's {full_spmv} SpMV steps"),
-                seconds_per_step=per_spmv)
+                sample=(f"first two restart cycles ({st['spmv_calls']} Lanczos steps, {dt:.2f} s) of the same solve "
+                        f"on {threads} threads; the remaining steps at the second cycle's "
+                        f"{per_step * 1e3:.1f} ms per step, to the {full_spmv} operator applications of {full_src}"),
+                seconds_per_step=per_step, sample_seconds=dt, extrapolated_seconds=est)
+
+
+def full_spmv_count(args, wl, gpu_count=None):
+    g = golden_of(args.workload)
+    if g is not None:
+        return int(g["spmv_calls"]), "the reference's own full CPU solve (tests/golden)"
+    if args.full_spmv:
+        return args.full_spmv, "--full-spmv"
+    return int(gpu_count or 0), "this library's solve of the same workload"
 
 
 def run_reference(args, wl, m):
@@ -223,10 +241,13 @@ def run_reference(args, wl, m):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    full = FULL_SOLVE_SPMV.get(args.workload) or args.full_spmv
+    full, src = full_spmv_count(args, wl)
+    if not full:
+        print(json.dumps({"impl": "reference", "unavailable": "no operator-application count for this workload"}))
+        return
     for _ in range(args.warmup):
-        cpu_sample(m, wl, threads, full)
-    vals = [cpu_sample(m, wl, threads, full) for _ in range(args.steps)]
+        cpu_sample(m, wl, threads, full, src)
+    vals = [cpu_sample(m, wl, threads, full, src) for _ in range(args.steps)]
     v = statistics.median(x["value"] for x in vals)
     secs = wl["nev"] / v
     line = {"metric": "converged eigenpairs/s (resid <= 1e-10 ||A||)", "value": v, "unit": "eigenpairs/s",
@@ -236,8 +257,38 @@ def run_reference(args, wl, m):
             "config": config_of(args, wl, m),
             "cpu_baseline": {"value": v, "unit": "eigenpairs/s", "cores": threads, "kind": "port",
                              "sample": vals[0]["sample"]},
+            "timing": {"step_is": "a bounded sample (two restart cycles) extrapolated to the full solve",
+                       "sample_seconds_median": statistics.median(x["sample_seconds"] for x in vals),
+                       "extrapolated_solve_seconds": secs},
             "e2e": {"value": v, "unit": "eigenpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_calibrate_cpu(args, wl, m):
+    """One full oracle solve on all host cores, with per-cycle timing, against
+    the two-cycle extrapolation of the reference arm."""
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    full, src = full_spmv_count(args, wl)
+    est = cpu_sample(m, wl, threads, full, src)
+    x0 = G.start_vector(m.n, 0)
+    t = time.perf_counter()
+    rc, vals, _, st = oracle.solve_csr(m.row_ptr, m.col, m.val, m.ncols, False, wl["nev"], wl["ncv"], x0,
+                                       tol=wl["tol"], threads=threads, trace=True)
+    dt = time.perf_counter() - t
+    tr = st.pop("trace")
+    out = {"workload": args.workload, "threads": threads, "rc": rc, "full_solve_seconds": dt,
+           "full_solve_spmv": st["spmv_calls"], "restarts": st["restarts"],
+           "reference_spmv": full, "reference_spmv_source": src,
+           "extrapolated_seconds": est["extrapolated_seconds"], "sample_seconds": est["sample_seconds"],
+           "extrapolation_error": est["extrapolated_seconds"] / dt - 1.0,
+           "cycles": {"seconds": [c[0] for c in tr], "spmv": [int(c[1]) for c in tr], "k": [int(c[2]) for c in tr]}}
+    g = golden_of(args.workload)
+    if g is not None and rc == 0:
+        ref = g["values"]
+        out["eigenvalue_rel_err_vs_reference"] = float(np.abs(vals[:wl["nev"]] - ref).max() / np.abs(ref).max())
+    print(json.dumps(out), flush=True)
 
 
 def batch_problems(count, seed=3):
@@ -248,67 +299,12 @@ def batch_problems(count, seed=3):
     return [G.banded_random(int(n), int(b), seed=seed, problem=i) for i, (n, b) in enumerate(zip(ns, bws))]
 
 
-def run_batch(args):
-    """Batched form vs the plain FP64 drop-in run one problem at a time."""
-    import torch
-
-    import hlanc_gb300 as H
-    from hlanc_gb300 import build
-    build.build()
-    mats = batch_problems(args.batch_count)
-    nev, ncv = 8, 24
-    out = {}
-    for mode, prec in (("fp64", H.HLANC_PREC_FP64), ("fp32_refine", H.HLANC_PREC_FP32_REFINE)):
-        ops = [H.dcsrmv_operator_gpu(m, precision=prec) for m in mats]
-        vals = [torch.zeros(ncv, dtype=torch.float64, device="cuda") for _ in mats]
-        vecs = [torch.zeros((ncv, m.n), dtype=torch.float64, device="cuda") for m in mats]
-        times = []
-        for rep in range(args.warmup + args.steps):
-            b = H.Batch(ops, nev, ncv, precision=prec, tol=1e-10)
-            torch.cuda.synchronize()
-            t = time.perf_counter()
-            status, st = b.run([v.data_ptr() for v in vals], [x.data_ptr() for x in vecs])
-            torch.cuda.synchronize()
-            dt = time.perf_counter() - t
-            b.close()
-            if rep >= args.warmup:
-                times.append(dt)
-        ok = int((status == 0).sum())
-        worst = 0.0
-        for m, op, v, x in zip(mats, ops, vals, vecs):
-            r, _ = H.residuals_device(op, nev, v.data_ptr(), x.data_ptr(), m.n)
-            worst = max(worst, float(r.max()) / float(np.abs(G.to_scipy(m)).sum(axis=1).max()))
-        t = statistics.median(times)
-        out[f"batched_{mode}"] = {"seconds": t, "eigenpairs_per_s": ok * nev / t, "converged": ok,
-                                  "max_residual_over_normA": worst, "spmv_calls": st["spmv_calls"]}
-        if mode == "fp64":
-            # plain FP64 drop-in, one solve after another (same GPU, same problems)
-            torch.cuda.synchronize()
-            t = time.perf_counter()
-            okp = 0
-            for m, op, v, x in zip(mats, ops, vals, vecs):
-                stp = H.solve_device(op, nev, ncv, v.data_ptr(), x.data_ptr(), m.n, tol=1e-10)
-                okp += stp["rc"] == 0
-            torch.cuda.synchronize()
-            tp = time.perf_counter() - t
-            out["plain_fp64_one_at_a_time"] = {"seconds": tp, "eigenpairs_per_s": okp * nev / tp, "converged": okp}
-        del ops
-    best = max(out["batched_fp64"]["eigenpairs_per_s"], out["batched_fp32_refine"]["eigenpairs_per_s"])
-    line = {"metric": "converged eigenpairs/s (resid <= 1e-10 ||A||), batched", "value":
-            out["batched_fp32_refine"]["eigenpairs_per_s"], "unit": "eigenpairs/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64 (fp32 SpMV)",
-            "data": "synthetic (seeded generator)",
-            "config": {"workload": f"batch{args.batch_count}", "nev": nev, "ncv": ncv, "tol": 1e-10,
-                       "matrices": "banded random, n log-uniform [2000,200000], half-bandwidth U{2..16}, seed 3"},
-            "results": out, "speedup_vs_plain_fp64": best / out["plain_fp64_one_at_a_time"]["eigenpairs_per_s"]}
-    print(json.dumps(line), flush=True)
-
-
-def serve_requests(count, seed=4, rate=200.0, n_lo=1000, n_hi=200000):
+def serve_requests(count, seed=4, rate=200.0, n_lo=1000, n_hi=2000000):
     """Poisson request stream: exponential inter-arrival times (mean 1/rate)
     from seed, n log-uniform in [n_lo, n_hi], generator uniform over the
     workloads' families, nev uniform in {4, 8, 16}, ncv = 3 nev, 70% FP32-SpMV
-    + refinement and 30% plain FP64."""
+    + refinement and 30% plain FP64.  The draws are counter-based, so the
+    first k requests of a longer stream are the same k requests."""
     u = G.uniform01(seed, 40, 6 * count).reshape(count, 6)
     arrivals = np.cumsum(-np.log(1.0 - u[:, 0]) / rate)
     reqs = []
@@ -331,20 +327,74 @@ def serve_requests(count, seed=4, rate=200.0, n_lo=1000, n_hi=200000):
     return reqs
 
 
-def run_serve(args):
+def _generate(kind, count, n_hi):
+    """Matrices of one of the other forms' workloads (runs in a spawned
+    process while the GPU measures the headline workload)."""
+    if kind == "c3":
+        return G.chung_lu_normalized(1 << 22, seed=2)
+    if kind == "c4":
+        return batch_problems(count)
+    return serve_requests(count, n_hi=n_hi)
+
+
+def batch_compare(H, mats, reps=1):
+    """512 banded problems: batched FP64, batched FP32 SpMV + FP64 refinement,
+    and the plain FP64 drop-in solving them one after another (same GPU)."""
+    import torch
+    nev, ncv = 8, 24
+    ops = [H.dcsrmv_operator_gpu(m, precision=H.HLANC_PREC_FP32_REFINE) for m in mats]
+    vals = [torch.zeros(ncv, dtype=torch.float64, device="cuda") for _ in mats]
+    vecs = [torch.zeros((ncv, m.n), dtype=torch.float64, device="cuda") for m in mats]
+    norms = [float(np.abs(G.to_scipy(m)).sum(axis=1).max()) for m in mats]
+    out = {}
+    for mode, prec in (("fp64", H.HLANC_PREC_FP64), ("fp32_refine", H.HLANC_PREC_FP32_REFINE)):
+        times = []
+        for rep in range(1 + reps):
+            b = H.Batch(ops, nev, ncv, precision=prec, tol=1e-10)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            status, st = b.run([v.data_ptr() for v in vals], [x.data_ptr() for x in vecs])
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t
+            b.close()
+            if rep >= 1:
+                times.append(dt)
+        ok = int((status == 0).sum())
+        worst = 0.0
+        for op, v, x, na, m in zip(ops, vals, vecs, norms, mats):
+            r, _ = H.residuals_device(op, nev, v.data_ptr(), x.data_ptr(), m.n)
+            worst = max(worst, float(r.max()) / na)
+        t = statistics.median(times)
+        out[f"batched_{mode}"] = {"seconds": t, "eigenpairs_per_s": ok * nev / t, "converged": ok,
+                                  "max_residual_over_normA": worst, "spmv_calls": st["spmv_calls"]}
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    okp = 0
+    for m, op, v, x in zip(mats, ops, vals, vecs):
+        stp = H.solve_device(op, nev, ncv, v.data_ptr(), x.data_ptr(), m.n, tol=1e-10)
+        okp += stp["rc"] == 0
+    torch.cuda.synchronize()
+    tp = time.perf_counter() - t
+    plain = okp * nev / tp
+    out["plain_fp64_one_at_a_time"] = {"seconds": tp, "eigenpairs_per_s": plain, "converged": okp}
+    out["speedup_fp64_vs_plain"] = out["batched_fp64"]["eigenpairs_per_s"] / plain
+    out["speedup_mixed_vs_plain"] = out["batched_fp32_refine"]["eigenpairs_per_s"] / plain
+    out["problems"] = len(mats)
+    out["config"] = {"nev": nev, "ncv": ncv, "tol": 1e-10,
+                     "matrices": "banded random, n log-uniform [2000,200000], half-bandwidth U{2..16}, seed 3"}
+    del ops
+    return out
+
+
+def serve_compare(H, reqs, slots=32, lanes=0, arms=("server", "server_all_fp64", "plain")):
     """Continuous-batching server vs the plain FP64 solver serving the same
-    stream one request at a time (FIFO); latency = completion - arrival.
-    The server also runs the stream with every request in FP64, to separate
-    the engine's gain from the precision mix."""
-    import hlanc_gb300 as H
-    from hlanc_gb300 import build
-    build.build()
-    reqs = serve_requests(args.serve_count, n_hi=args.serve_nmax)
+    stream one request at a time (FIFO); latency = completion - arrival.  The
+    server also runs the stream with every request in FP64, to separate the
+    engine's gain from the precision mix."""
     for r in reqs:
         prec = H.HLANC_PREC_FP32_REFINE if r["mixed"] else H.HLANC_PREC_FP64
         r["op"] = H.dcsrmv_operator_gpu(r["m"], precision=prec)
-    # warm-up: a few solves to load kernels
-    for r in reqs[:3]:
+    for r in reqs[:3]:           # load the kernels
         H.solve(r["op"], r["nev"], r["ncv"], tol=1e-10)
 
     def stats(lat, t_total, ok_pairs, ok):
@@ -354,7 +404,7 @@ def run_serve(args):
                 "p99_s": float(np.percentile(lat, 99))}
 
     def serve(all_fp64):
-        srv = H.Server(mem_budget_bytes=150 << 30, max_slots=args.serve_slots, lanes=args.serve_lanes)
+        srv = H.Server(mem_budget_bytes=150 << 30, max_slots=slots, lanes=lanes)
         t0 = time.perf_counter()
         nxt, ids, done, lat, pairs, ok = 0, {}, set(), [], 0, 0
         while len(done) < len(reqs):
@@ -382,41 +432,107 @@ def run_serve(args):
         srv.close()
         return out
 
-    served = serve(False)
-    served_fp64 = serve(True)
-    # plain FP64, one at a time, FIFO over the same arrivals
-    t0 = time.perf_counter()
-    lat, pairs, ok = [], 0, 0
+    out = {}
+    if "server" in arms:
+        out["server"] = serve(False)
+    if "server_all_fp64" in arms:
+        out["server_all_fp64"] = serve(True)
+    if "plain" in arms:
+        t0 = time.perf_counter()
+        lat, pairs, ok = [], 0, 0
+        for r in reqs:
+            now = time.perf_counter() - t0
+            if r["t"] > now:
+                time.sleep(r["t"] - now)
+            rc, _, _, _ = H.solve(r["op"], r["nev"], r["ncv"], tol=1e-10)
+            lat.append(time.perf_counter() - t0 - r["t"])
+            pairs += r["nev"] if rc == 0 else 0
+            ok += rc == 0
+        out["plain_fp64_one_at_a_time"] = stats(lat, time.perf_counter() - t0, pairs, ok)
+        plain = out["plain_fp64_one_at_a_time"]
+        for k in ("server", "server_all_fp64"):
+            if k in out:
+                out[f"throughput_ratio_{k}"] = out[k]["eigenpairs_per_s"] / plain["eigenpairs_per_s"]
+                out[f"p99_ratio_plain_over_{k}"] = plain["p99_s"] / out[k]["p99_s"]
     for r in reqs:
-        now = time.perf_counter() - t0
-        if r["t"] > now:
-            time.sleep(r["t"] - now)
-        rc, _, _, _ = H.solve(r["op"], r["nev"], r["ncv"], tol=1e-10)
-        lat.append(time.perf_counter() - t0 - r["t"])
-        pairs += r["nev"] if rc == 0 else 0
-        ok += rc == 0
-    plain = stats(lat, time.perf_counter() - t0, pairs, ok)
-    line = {"metric": "serving throughput (eigenpairs/s) and latency", "value": served["eigenpairs_per_s"],
+        r.pop("op", None)
+    return out
+
+
+def c3_compare(H, m, golden):
+    """The Chung-Lu graph n = 2^22 (nev 16, ncv 48) in plain FP64 and in
+    mixed precision, each pair against the reference's own CPU solve."""
+    import torch
+    nev, ncv = 16, 48
+    op = H.dcsrmv_operator_gpu(m, precision=H.HLANC_PREC_FP32_REFINE)
+    norm_a = float(np.abs(G.to_scipy(m)).sum(axis=1).max())
+    out = {}
+    for mode, prec in (("fp64", H.HLANC_PREC_FP64), ("fp32_refine", H.HLANC_PREC_FP32_REFINE)):
+        vals = torch.zeros(ncv, dtype=torch.float64, device="cuda")
+        vecs = torch.zeros((ncv, m.n), dtype=torch.float64, device="cuda")
+        times = []
+        for rep in range(3):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            st = H.solve_device(op, nev, ncv, vals.data_ptr(), vecs.data_ptr(), m.n, tol=1e-10, precision=prec)
+            torch.cuda.synchronize()
+            if rep:
+                times.append(time.perf_counter() - t)
+        res, _ = H.residuals_device(op, nev, vals.data_ptr(), vecs.data_ptr(), m.n)
+        lam = vals[:nev].cpu().numpy()
+        d = {"seconds": statistics.median(times), "rc": st["rc"], "spmv_calls": st["spmv_calls"],
+             "restarts": st["restarts"], "refine_restarts": st["refine_restarts"],
+             "residual_over_normA": [float(r / norm_a) for r in res]}
+        d["eigenpairs_per_s"] = nev / d["seconds"] if st["rc"] == 0 and res.max() <= 1e-10 * norm_a else 0.0
+        if golden is not None:
+            ref = golden["values"]
+            d["eigenvalue_rel_err_vs_reference"] = [float(abs(a - b) / abs(b)) for a, b in zip(lam, ref)]
+        out[mode] = d
+    out["mixed_over_fp64"] = out["fp32_refine"]["eigenpairs_per_s"] / max(out["fp64"]["eigenpairs_per_s"], 1e-30)
+    out["reference"] = ("eigenvalues of the reference's own CPU solve (ds_solver_mkl, same start vector), "
+                        "tests/golden/c3_chunglu_2e22.npz" if golden is not None else "not generated")
+    return out
+
+
+def run_batch(args):
+    import hlanc_gb300 as H
+    from hlanc_gb300 import build
+    build.build()
+    out = batch_compare(H, batch_problems(args.batch_count), reps=max(args.steps, 1))
+    line = {"metric": "converged eigenpairs/s (resid <= 1e-10 ||A||), batched",
+            "value": out["batched_fp32_refine"]["eigenpairs_per_s"], "unit": "eigenpairs/s", "n_gpus": 1,
+            "steps": args.steps, "higher_is_better": True, "dtype": "f64 (fp32 SpMV)",
+            "data": "synthetic (seeded generator)", "config": {"workload": f"batch{args.batch_count}"}, **out}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    import hlanc_gb300 as H
+    from hlanc_gb300 import build
+    build.build()
+    reqs = serve_requests(args.serve_count, n_hi=args.serve_nmax)
+    out = serve_compare(H, reqs, args.serve_slots, args.serve_lanes)
+    line = {"metric": "serving throughput (eigenpairs/s) and latency", "value": out["server"]["eigenpairs_per_s"],
             "unit": "eigenpairs/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64 (70% fp32 SpMV)",
             "data": "synthetic (seeded generators)",
             "config": {"workload": f"serve{args.serve_count}", "arrivals": "Poisson, mean 200 req/s, seed 4",
                        "n": f"log-uniform [1000, {args.serve_nmax}]", "nev": "{4,8,16}, ncv = 3 nev",
                        "mix": "70% fp32+refine", "tol": 1e-10, "max_restarts": 200,
-                       "slots": args.serve_slots, "lanes": args.serve_lanes or 2, "mem_budget_GB": 150},
-            "server": served, "server_all_fp64": served_fp64, "plain_fp64_one_at_a_time": plain,
-            "throughput_ratio": served["eigenpairs_per_s"] / plain["eigenpairs_per_s"],
-            "throughput_ratio_all_fp64": served_fp64["eigenpairs_per_s"] / plain["eigenpairs_per_s"],
-            "p99_ratio_plain_over_server": plain["p99_s"] / served["p99_s"]}
+                       "slots": args.serve_slots, "lanes": args.serve_lanes or 2, "mem_budget_GB": 150,
+                       "stream": "the first requests of the seed-4 stream of 20,000"}, **out}
     print(json.dumps(line), flush=True)
 
 
 def config_of(args, wl, m):
+    ws = 12.0 * m.nnz + 8.0 * m.n * (wl["ncv"] * 1.5 + 4)
+    l2 = ("inputs larger than L2 (CSR + basis %.2f GB >> 129 MB); no flush needed" % (ws / 1e9) if ws > 4 * 129e6
+          else "working set %.1f MB fits in L2 (129 MB); not flushed between solves: latency-bound, "
+               "as in repeated solves of a small problem" % (ws / 1e6))
     return {"workload": args.workload, "description": wl["desc"], "n": m.n, "nnz": m.nnz, "nev": wl["nev"],
             "ncv": wl["ncv"], "tol": wl["tol"] or "dlamch(E)", "which": "largest algebraic",
             "start": "uniform[-1,1) seed 0",
             "precision": "fp32 SpMV + fp64 refinement" if wl.get("mixed") else "fp64",
-            "l2": "inputs larger than L2 (CSR + basis >> 129 MB); no flush needed",
-            "parallelism": "replicas"}
+            "l2": l2, "parallelism": "replicas"}
 
 
 def main():
@@ -429,13 +545,16 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--full-spmv", type=int, default=0, help="SpMV count of a full solve (CPU extrapolation)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--batch", action="store_true", help="batched form (512 banded problems)")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched / serving / mixed workloads")
+    ap.add_argument("--forms-serve-count", type=int, default=100, help="requests of the serving slice")
+    ap.add_argument("--calibrate-cpu", action="store_true", help="full oracle solve vs the CPU extrapolation")
+    ap.add_argument("--batch", action="store_true", help="batched form alone (512 banded problems)")
     ap.add_argument("--batch-count", type=int, default=512)
-    ap.add_argument("--serve", action="store_true", help="serving form (Poisson request stream)")
+    ap.add_argument("--serve", action="store_true", help="serving form alone (Poisson request stream)")
     ap.add_argument("--serve-count", type=int, default=100)
     ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--serve-lanes", type=int, default=0, help="server launch lanes (0 = library default)")
-    ap.add_argument("--serve-nmax", type=int, default=200000, help="largest n of the request stream")
+    ap.add_argument("--serve-nmax", type=int, default=2000000, help="largest n of the request stream")
     args = ap.parse_args()
     if args.batch:
         run_batch(args)
@@ -448,6 +567,21 @@ def main():
     if args.impl == "reference":
         run_reference(args, wl, m)
         return
+    if args.calibrate_cpu:
+        run_calibrate_cpu(args, wl, m)
+        return
+
+    rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
+    forms = not args.no_forms and world == 1 and rank == 0
+    pool, pending = None, {}
+    if forms:
+        # the other forms' matrices, built on host cores while the GPU measures
+        import multiprocessing as mp
+        pool = mp.get_context("spawn").Pool(3)
+        pending = {"c3": pool.apply_async(_generate, ("c3", 0, 0)),
+                   "c4": pool.apply_async(_generate, ("c4", 512, 0)),
+                   "c5": pool.apply_async(_generate, ("c5", args.forms_serve_count, 2000000))}
+        pool.close()
 
     import torch
 
@@ -490,21 +624,18 @@ def main():
     res, rdiff = H.residuals_device(op, nev, vals.data_ptr(), vecs.data_ptr(), m.n)
     valid = all(s["rc"] == 0 and s["nconv"] >= nev for s in stats) and float(res.max()) <= 1e-10 * norm_a
     value = replica_value(world, nev, ms) if valid else 0.0
-    mixed_cmp = None
-    if prec == H.HLANC_PREC_FP32_REFINE:
-        # per-eigenpair comparison of the mixed-precision pairs with a plain FP64 solve
-        vals64 = torch.zeros(ncv, dtype=torch.float64, device="cuda")
-        vecs64 = torch.zeros((ncv, m.n), dtype=torch.float64, device="cuda")
-        H.solve_device(op, nev, ncv, vals64.data_ptr(), vecs64.data_ptr(), m.n, dev=dev, tol=tol,
-                       stream=stream.cuda_stream, precision=H.HLANC_PREC_FP64)
-        torch.cuda.synchronize()
-        l_mix, l_64 = vals[:nev].double().cpu().numpy(), vals64[:nev].double().cpu().numpy()
-        dots = torch.abs((vecs[:nev] * vecs64[:nev]).sum(dim=1)).cpu().numpy()
-        mixed_cmp = {"eigenvalue_rel_diff": [float(abs(a - b) / abs(b)) for a, b in zip(l_mix, l_64)],
-                     "residual_over_normA": [float(r / norm_a) for r in res],
-                     "abs_dot_with_fp64_vector": [float(d) for d in dots],
-                     "note": "pair i of the FP32-SpMV + FP64-refinement solve against pair i of a plain FP64 solve "
-                             "(same start vector); |<v, v64>| near 1 where the eigenvalue is simple"}
+    parity = None
+    g = golden_of(args.workload)
+    if g is not None:
+        lam = vals[:nev].cpu().numpy()
+        ref = g["values"]
+        err = np.abs(lam - ref) / np.abs(ref)
+        parity = {"eigenvalue_rel_err_vs_reference_max": float(err.max()),
+                  "eigenvalue_rel_err_vs_reference": [float(x) for x in err],
+                  "reference_spmv_calls": int(g["spmv_calls"]),
+                  "reference": "the reference's own CPU solver (ds_solver_mkl + dcsrmv_operator_mkl) on the same "
+                               "matrix and start vector, tests/golden/%s.npz" % GOLDEN_OF[args.workload],
+                  "tolerance": 1e-10, "within_tolerance": bool(err.max() <= 1e-10)}
 
     # end to end through the C ABI with host buffers in pinned memory: the
     # operator is built from host CSR arrays, the solve returns its pairs to
@@ -585,23 +716,34 @@ def main():
     ratio = read_traffic_ratio(dom)
     traffic = ratio * d["bytes"] / max(d["launches"], 1) if ratio else None
     # share of the dominant kernel's multiply-adds issued as FP64 FMAs: the
-    # hybrid CGS kernels run 5 of every 8 projection columns and about half
-    # of the update columns in FP64, the rest as exact integer products
-    hybrid = m.n >= H.CGS_HYBRID_MIN_ROWS and dom in ("cgs_proj", "cgs_apply")
-    fp64_share = cgs_fp64_share(dom, nev, ncv) if hybrid else 1.0
+    # hybrid projection runs 5 of every 8 columns in FP64 and the rest as
+    # exact integer products; the update runs only its large-coefficient
+    # columns in FP64 and the rest in FP32 from the basis copy
+    hybrid = m.n >= H.CGS_HYBRID_MIN_ROWS
+    if dom == "cgs_proj":
+        fp64_share = cgs_fp64_share(dom, nev, ncv) if hybrid else 1.0
+    elif dom == "cgs_apply":
+        fp64_share = 1.0 - pst.get("cgs_update_fp32_share", 0.0)
+    else:
+        fp64_share = 1.0
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "traffic": traffic, "traffic_source": "ncu dram bytes / algorithmic bytes (profiles/) x "
                                                           "algorithmic bytes per launch" if ratio else None,
                 "bytes_per_launch": d["bytes"] / max(d["launches"], 1),
                 "avg_launch_ms": d["ms"] / max(d["launches"], 1),
-                "cgs_kernels": "hybrid FP64 + exact integer" if hybrid else "fp64",
+                "cgs_kernels": ("hybrid FP64 + exact integer projection; update with the FP32 basis copy for "
+                                "small coefficients" if hybrid else "FP64 projection; update with the FP32 basis "
+                                "copy for small coefficients"),
+                "cgs_update_fp32_share": pst.get("cgs_update_fp32_share"),
                 "fp64": {"achieved_tflops": fp64_share * d["flops"] / (d["ms"] * 1e-3) / 1e12 if d["ms"] else 0.0,
                          "peak_tflops": fp64_peak,
                          "frac": (fp64_share * d["flops"] / (d["ms"] * 1e-3) / 1e12) / fp64_peak if d["ms"] else 0.0,
                          "fp64_share_of_flops": fp64_share,
                          "peak_source": "measured live (hlanc_diag_fp64_tflops)"},
                 "time_share": {k: prof[k]["ms"] / total_kernel_ms for k in kernel_classes + ["aux"]},
+                "achieved_gbs_by_class": {k: prof[k]["bytes"] / (prof[k]["ms"] * 1e-3) / 1e9 if prof[k]["ms"] else 0.0
+                                          for k in kernel_classes},
                 "host_restart_ms": prof["host_restart"]["ms"]}
     line = {"metric": "converged eigenpairs/s (resid <= 1e-10 ||A||)", "value": value, "unit": "eigenpairs/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -615,7 +757,7 @@ def main():
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
                     "host_buffers": "pinned", "breakdown": e2e_parts[-1]},
             "roofline": roofline, "gpu_launches": launches, "clocks": clk.summary(),
-            **({"mixed_vs_fp64": mixed_cmp} if mixed_cmp else {}),
+            **({"parity": parity} if parity else {}),
             "spmv": {"us_per_call": spmv_ms * 1e3, "bytes_per_call": spmv_bytes,
                      "achieved_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9,
                      "frac_of_hbm": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / measured_peaks()[0],
@@ -624,9 +766,37 @@ def main():
                      "note": "FP64 CSR SpMV alone, algorithmic bytes 12 nnz + 4(n+1) + 16 n; back-to-back calls "
                              "(the CSR arrays exceed L2, x/y may stay in it) and, separately, each call after a "
                              "256 MB L2 flush"}}
+    del op, vals, vecs
+    if forms:
+        # the batched, serving and mixed-precision forms on the same GPU (not
+        # part of the timed solves above)
+        fr = {"note": "after the timed solves; each form against the plain FP64 drop-in on the same GPU"}
+        t_forms = time.perf_counter()
+        try:
+            fr["c3_chunglu_2e22"] = c3_compare(H, pending["c3"].get(), golden_of("chunglu_22"))
+        except Exception as e:  # noqa: BLE001 - reported in the line, the headline stands
+            fr["c3_chunglu_2e22"] = {"error": repr(e)}
+        try:
+            fr["c4_batched_512"] = batch_compare(H, pending["c4"].get())
+        except Exception as e:  # noqa: BLE001
+            fr["c4_batched_512"] = {"error": repr(e)}
+        try:
+            reqs = pending["c5"].get()
+            fr["c5_serving"] = serve_compare(H, reqs)
+            fr["c5_serving"]["config"] = {
+                "requests": len(reqs), "stream": "the first %d requests of the seed-4 stream of 20,000 "
+                "(Poisson, mean 200 req/s)" % len(reqs), "n": "log-uniform [1000, 2000000]",
+                "nev": "{4,8,16}, ncv = 3 nev", "mix": "70% fp32+refine / 30% fp64", "mem_budget_GB": 150,
+                "slots": 32}
+        except Exception as e:  # noqa: BLE001
+            fr["c5_serving"] = {"error": repr(e)}
+        fr["seconds"] = time.perf_counter() - t_forms
+        line["forms"] = fr
+    if pool is not None:
+        pool.terminate()
     if rank == 0 and world == 1 and not args.no_cpu:
-        full = FULL_SOLVE_SPMV.get(args.workload) or stats[-1]["spmv_calls"]
-        line["cpu_baseline"] = cpu_sample(m, wl, os.cpu_count() or 1, full)
+        full, src = full_spmv_count(args, wl, stats[-1]["spmv_calls"])
+        line["cpu_baseline"] = cpu_sample(m, wl, os.cpu_count() or 1, full, src)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg is not None:

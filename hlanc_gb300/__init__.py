@@ -34,6 +34,8 @@ HLANC_CGS_HYBRID = 2
 CGS_HYBRID_MIN_ROWS = 1 << 18     # HLANC_CGS_AUTO picks the hybrid kernels from this many rows
 HLANC_MAX_NCV = 128
 HLANC_MAX_NEV = 63
+# kernel variants counted by hlanc_kernel_launches_of
+KL_ALL, KL_PROJ_HYBRID, KL_PROJ_FP64, KL_APPLY_SHADOW, KL_APPLY_FP64, KL_BASIS_TC, KL_BASIS_FP64 = range(7)
 
 _lib = None
 
@@ -49,14 +51,16 @@ class Opts(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_restarts", C.c_int), ("precision", C.c_int),
                 ("seed", C.c_ulonglong), ("start", C.POINTER(C.c_double)), ("stream", C.c_void_p),
                 ("use_graphs", C.c_int), ("restart_on_device", C.c_int), ("profile", C.c_int),
-                ("basis_kernel", C.c_int), ("cgs_kernel", C.c_int), ("reserved", C.c_int * 3)]
+                ("basis_kernel", C.c_int), ("cgs_kernel", C.c_int), ("wait_limit", C.c_int),
+                ("reserved", C.c_int * 2)]
 
 
 class Stats(C.Structure):
     _fields_ = [("spmv_calls", C.c_longlong), ("cgs_passes", C.c_longlong), ("restarts", C.c_int),
                 ("nconv", C.c_int), ("refine_restarts", C.c_int), ("status", C.c_int),
                 ("rnorm", C.c_double), ("seconds", C.c_double), ("bytes_spmv", C.c_double),
-                ("bytes_cgs", C.c_double), ("bytes_restart", C.c_double), ("reserved", C.c_double * 4)]
+                ("bytes_cgs", C.c_double), ("bytes_restart", C.c_double), ("cgs_update_fp32_share", C.c_double),
+                ("reserved", C.c_double * 3)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -101,6 +105,7 @@ def _declare(L):
         "hlanc_status_string": (C.c_char_p, [_i]),
         "hlanc_version": (_i, [_ip, _ip]),
         "hlanc_kernel_launches": (C.c_longlong, []),
+        "hlanc_kernel_launches_of": (C.c_longlong, [_i]),
         "hlanc_opts_default": (None, [C.POINTER(Opts)]),
         "hlanc_matrix_read": (_i, [C.c_char_p, C.c_char_p, _i, C.POINTER(_p)]),
         "hlanc_matrix_create": (_i, [_i, _i, _i, _p, _p, _p, _i, C.POINTER(_p)]),
@@ -161,11 +166,12 @@ def _check(rc: int, what: str) -> None:
 def opts(tol: float = 0.0, max_restarts: int = 200, precision: int = HLANC_PREC_FP64, seed: int = 0,
          start: Optional[np.ndarray] = None, stream: int = 0, use_graphs: bool = True,
          restart_on_device: bool = False, profile: bool = False, basis_fp64: bool = False,
-         cgs: int = HLANC_CGS_AUTO):
+         cgs: int = HLANC_CGS_AUTO, wait_limit: int = 0):
     o = Opts()
     lib().hlanc_opts_default(C.byref(o))
     o.basis_kernel = HLANC_BASIS_FP64 if basis_fp64 else HLANC_BASIS_AUTO
     o.cgs_kernel = cgs
+    o.wait_limit = wait_limit
     o.tol, o.max_restarts, o.precision, o.seed = tol, max_restarts, precision, seed
     o.use_graphs = int(use_graphs)
     o.restart_on_device = int(restart_on_device)
@@ -408,6 +414,16 @@ def read_eigs(filename: str):
 
 def kernel_launches() -> int:
     return int(lib().hlanc_kernel_launches())
+
+
+def kernel_launches_of(kind: int) -> int:
+    """Launches since load of one kernel variant (KL_*)."""
+    return int(lib().hlanc_kernel_launches_of(kind))
+
+
+def variant_counts() -> dict:
+    names = ("all", "proj_hybrid", "proj_fp64", "apply_shadow", "apply_fp64", "basis_tc", "basis_fp64")
+    return {nm: kernel_launches_of(i) for i, nm in enumerate(names)}
 
 
 def fp64_peak_tflops(dev: int = 0) -> float:

@@ -185,6 +185,7 @@ struct ProbRes {
     void *host_ctx = nullptr;
     double *block = nullptr;   // V | r0 | r1 | part | gpart | small
     double *V = nullptr, *r0 = nullptr, *r1 = nullptr, *part = nullptr, *gpart = nullptr, *small = nullptr;
+    float *V32 = nullptr;      // FP32 shadow of V (ld x ncv)
     State *st = nullptr;
     unsigned *counter = nullptr;
     float *x32 = nullptr;
@@ -209,6 +210,7 @@ struct ProbRes {
         size_t d = ld * ncv + 2 * ld + (nt + ng) * pst + SM_SIZE(ncv);
         size_t b = d * sizeof(double) + 1024 + 4 * ng;
         if (fp32) b += ld * sizeof(float);
+        b += ld * ncv * sizeof(float);    // FP32 shadow of the basis
         b += ld * ncv * sizeof(double);   // Ritz output
         return b;
     }
@@ -252,6 +254,9 @@ struct ProbRes {
             CK(cudaMemsetAsync(x32, 0, (size_t)ld * sizeof(float), s));
             bytes += (size_t)ld * sizeof(float);
         }
+        CK(dmalloc((void **)&V32, (size_t)ld * ncv * sizeof(float), s));
+        CK(cudaMemsetAsync(V32, 0, (size_t)ld * ncv * sizeof(float), s));
+        bytes += (size_t)ld * ncv * sizeof(float);
         h.assign(2 * ncv, 0.0);
         ritz_s.assign(ncv, 0.0);
         bnds_s.assign(ncv, 0.0);
@@ -270,8 +275,9 @@ struct ProbRes {
         dfree(block);
         dfree(st);
         dfree(x32);
+        dfree(V32);
         if (own_vout) dfree(vout);
-        block = nullptr; st = nullptr; x32 = nullptr; vout = nullptr; own_vout = false;
+        block = nullptr; st = nullptr; x32 = nullptr; V32 = nullptr; vout = nullptr; own_vout = false;
         live = false;
     }
 };
@@ -292,6 +298,7 @@ State initial_state(int nev, int ncv, const hlanc_opts_t &o) {
     const double eps = 1.1102230246251565e-16;   // dlamch("E") = 2^-53
     S.tol = o.tol > 0.0 ? o.tol : eps;
     S.eps23 = pow(eps, 0.66666666666666663);      // HLanc.hpp:1652
+    S.wait_limit = o.wait_limit;
     return S;
 }
 
@@ -390,8 +397,9 @@ public:
     // 10,000-row Laplacian solve took 100.6 ms hybrid against 90.1 ms FP64;
     // the 4.1M-row solve 4.95 s against 5.41 s).
     static constexpr long long CGS_HYBRID_MIN_ROWS = 1 << 18;
-    bool hybrid_cgs() const {
-        return cgs_mode == HLANC_CGS_HYBRID || (cgs_mode == HLANC_CGS_AUTO && rows_active >= CGS_HYBRID_MIN_ROWS);
+    int cgs_flags() const {
+        const bool hy = cgs_mode == HLANC_CGS_HYBRID || (cgs_mode == HLANC_CGS_AUTO && rows_active >= CGS_HYBRID_MIN_ROWS);
+        return (hy ? CGS_PROJ_HYBRID : 0) | (cgs_mode != HLANC_CGS_FP64 ? CGS_APPLY_SHADOW : 0);
     }
 
     // Rebuild the descriptor/tile tables and the mailbox layout for `active`.
@@ -416,7 +424,7 @@ public:
             q.n = p.n; q.ld = p.ld; q.ncv = p.ncv; q.nev0 = p.nev0;
             q.tile0 = (int)T.size(); q.ntiles = p.ntiles;
             q.fp32 = p.fp32; q.pstride = p.pstride;
-            q.V = p.V; q.r0 = p.r0; q.r1 = p.r1; q.part = p.part; q.gpart = p.gpart; q.counter = p.counter;
+            q.V = p.V; q.V32 = p.V32; q.r0 = p.r0; q.r1 = p.r1; q.part = p.part; q.gpart = p.gpart; q.counter = p.counter;
             q.st = p.st; q.small = p.small;
             q.wext = p.csr ? nullptr : p.r0;     // non-null marks the host-operator path
             q.vout = p.vout; q.ldo = p.ldo;
@@ -487,6 +495,14 @@ public:
         return HLANC_OK;
     }
 
+    // A bounded device wait that gave up leaves State::err set; the host
+    // reads it with the State after every cycle and abandons the solve.
+    int device_error() const {
+        for (int p : active)
+            if (probs[p].hs.err != DEV_ERR_NONE) return HLANC_ERR_DEVICE_TIMEOUT;
+        return HLANC_OK;
+    }
+
     int slot_of(int prob) const {
         for (size_t a = 0; a < active.size(); ++a)
             if (active[a] == prob) return (int)a;
@@ -526,7 +542,7 @@ public:
         const int na = (int)active.size();
         if (!device_restart) launch_scatter(P_d, na, off_d, flag_d, mbox_d, stream);
         if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), basis_tc, stream);
-        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, hybrid_cgs(), one(), one_tr,
+        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, cgs_flags(), one(), one_tr,
                                                     stream);
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
@@ -622,7 +638,7 @@ public:
             if (p.host_op(p.host_ctx, xs_h, ys_h) != 0) return HLANC_ERR_CALLBACK;
             double *w = ((j + 1) & 1) ? p.r1 : p.r0;
             CK(cudaMemcpyAsync(w, ys_h, sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
-            launch_step(P_d, T_d, ntiles, S_d, nstiles, s, false, true, hybrid_cgs(), one(), one_tr, stream);
+            launch_step(P_d, T_d, ntiles, S_d, nstiles, s, false, true, cgs_flags(), one(), one_tr, stream);
         }
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
@@ -751,6 +767,7 @@ int drive(Engine &E) {
     for (;;) {
         int rc = host_path ? E.run_cycle_host(E.active[0], steps, basis_nev) : E.run_cycle(steps, basis_nev);
         if (rc) return rc;
+        if ((rc = E.device_error())) return rc;
         int running, nev_max, np_max;
         E.host_restarts(&running, &nev_max, &np_max);
         if (!running) break;
@@ -785,8 +802,10 @@ void fill_stats(hlanc_stats_t *stats, const State &S, const ProbRes &p, double n
     const double spmv_b = fp32 ? (8.0 * nnz + 4.0 * (n + 1) + 8.0 * n + 16.0 * n)
                                : (12.0 * nnz + 4.0 * (n + 1) + 16.0 * n + 16.0 * n);
     stats->bytes_spmv = spmv_b * (double)S.spmv;
-    stats->bytes_cgs = 16.0 * n * (double)S.sumc + 24.0 * n * (double)S.passes;
+    // projection 8 n c + 8 n; update 8 n (c - t) + 4 n t + 16 n (t columns from the FP32 copy)
+    stats->bytes_cgs = 16.0 * n * (double)S.sumc - 4.0 * n * (double)S.sumt + 24.0 * n * (double)S.passes;
     stats->bytes_restart = (8.0 * n * p.ncv + 16.0 * n) * S.napply + 8.0 * n * (double)S.sumnev;
+    stats->cgs_update_fp32_share = S.sumc > 0 ? (double)S.sumt / (double)S.sumc : 0.0;
 }
 
 void fill_profile(const State &S, const ProbRes &p, double nnz, int fp32) {
@@ -805,7 +824,7 @@ void fill_profile(const State &S, const ProbRes &p, double nnz, int fp32) {
     P.flops[KC_SPMV] = 2.0 * nnz * S.spmv;
     P.bytes[KC_PROJ] = 8.0 * n * S.sumc + 8.0 * n * S.passes;
     P.flops[KC_PROJ] = 2.0 * n * S.sumc;
-    P.bytes[KC_APPLY] = 8.0 * n * S.sumc + 16.0 * n * S.passes;
+    P.bytes[KC_APPLY] = 8.0 * n * (S.sumc - S.sumt) + 4.0 * n * S.sumt + 16.0 * n * S.passes;
     P.flops[KC_APPLY] = 2.0 * n * S.sumc + 2.0 * n * S.passes;
     P.bytes[KC_BASIS] = (8.0 * n * m + 16.0 * n) * S.napply + 8.0 * n * S.sumnev;
     P.flops[KC_BASIS] = 2.0 * n * m * (S.sumnev + S.napply);
@@ -919,6 +938,7 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
         S.spmv += S1.spmv;
         S.passes += S1.passes;
         S.sumc += S1.sumc;
+        S.sumt += S1.sumt;
         S.sumnev += S1.sumnev;
         S.napply += S1.napply;
     }
@@ -990,6 +1010,12 @@ int hlanc_version(int *major, int *minor) {
 }
 
 long long hlanc_kernel_launches(void) { return launch_counter().load(); }
+
+long long hlanc_kernel_launches_of(int kind) {
+    if (kind == HLANC_KL_ALL) return launch_counter().load();
+    if (kind < 0 || kind >= HLANC_KL_KINDS) return -1;
+    return variant_counter(kind).load();
+}
 
 void hlanc_opts_default(hlanc_opts_t *o) {
     memset(o, 0, sizeof(*o));
@@ -1374,7 +1400,14 @@ int hlanc_diag_cgs(int dev, int n, int c, int cgs_kernel, int reps, double *ms3)
     cudaEvent_t e0 = ev.e0, e1 = ev.e1;
     const bool hy = cgs_kernel == HLANC_CGS_HYBRID;
     const int pass_of[3] = {1, 2, 2}, which_of[3] = {0, 0, 1};
+    // update coefficients at the level of a second pass (1e-13 ||w||), so the
+    // FP32-copy update reads the copy for every column
+    std::vector<double> hsmall((size_t)c);
+    for (int i = 0; i < c; ++i) hsmall[i] = 1e-13 * sqrt((double)n) * (((i * 7) % 5) - 2) / 2.0;
     for (int q = 0; q < 3; ++q) {
+        if (which_of[q] == 1)
+            CK(cudaMemcpyAsync(p.small + SM_HV(c), hsmall.data(), sizeof(double) * c, cudaMemcpyHostToDevice,
+                               E.stream));
         for (int w = 0; w < 2; ++w)
             launch_cgs_kernel(E.P_d, E.T_d, E.ntiles, E.one(), E.one_tr, 0, pass_of[q], which_of[q], hy, E.stream);
         CK(cudaEventRecord(e0, E.stream));
@@ -1504,7 +1537,7 @@ int hlanc_batch_run(hlanc_batch_t b, double **values_d, double **vectors_d, int 
         ProbRes &p = E.probs[b->idx[q]];
         State S = p.hs;
         if (fp32) {
-            S.spmv += first[q].spmv; S.passes += first[q].passes; S.sumc += first[q].sumc;
+            S.spmv += first[q].spmv; S.passes += first[q].passes; S.sumc += first[q].sumc; S.sumt += first[q].sumt;
             S.sumnev += first[q].sumnev; S.napply += first[q].napply;
         }
         const int st = map_status(S.status);
@@ -1613,7 +1646,7 @@ void srv_finish(Srv &s, Srv::Lane &L, Srv::Request &r, int status) {
     const bool mixed = r.o.precision == HLANC_PREC_FP32_REFINE;
     if (mixed) {
         refine = S.iter;
-        S.spmv += r.first.spmv; S.passes += r.first.passes; S.sumc += r.first.sumc;
+        S.spmv += r.first.spmv; S.passes += r.first.passes; S.sumc += r.first.sumc; S.sumt += r.first.sumt;
         S.sumnev += r.first.sumnev; S.napply += r.first.napply;
     }
     r.status = status;
@@ -1663,6 +1696,13 @@ int srv_complete(Srv &s, Srv::Lane &L) {
     for (long long id : L.ids) {
         Srv::Request &r = s.reqs[id];
         ProbRes &p = E.probs[r.prob];
+        if (p.hs.err != DEV_ERR_NONE) {            // a bounded device wait gave up
+            r.finishing = false;
+            p.hs.status = ST_FAILED;               // no host restart for it below
+            p.hs.phase = PH_DONE;
+            srv_finish(s, L, r, HLANC_ERR_DEVICE_TIMEOUT);
+            continue;
+        }
         if (!r.finishing) { keep.push_back(id); continue; }
         r.finishing = false;
         if (p.hs.fin != 2) {                       // not produced: report, do not guess
@@ -1826,7 +1866,7 @@ int srv_launch(Srv &s, Srv::Lane &L) {
     if (basis_nev > 0)
         launch_basis(E.P_d, E.T_d, E.ntiles, E.max_ncv, Engine::basis_bucket(basis_nev), E.basis_tc, E.stream);
     for (int k = 0; k < steps; ++k)
-        launch_step(E.P_d, E.T_d, E.ntiles, E.S_d, E.nstiles, k, E.fp32_any, false, E.hybrid_cgs(), E.one(),
+        launch_step(E.P_d, E.T_d, E.ntiles, E.S_d, E.nstiles, k, E.fp32_any, false, E.cgs_flags(), E.one(),
                     E.one_tr, E.stream);
     launch_gather(E.P_d, na, E.off_d, E.mbox_d, E.stream);
     if ((rc = E.pull_async())) return rc;

@@ -4,6 +4,9 @@
 // implicitly restarted Lanczos loop touches lives in HBM for the whole solve:
 //   V      ld x ncv FP64 basis, column-major, ld = n rounded up to 64 rows
 //          (512-byte aligned columns; padding rows stay zero),
+//   V32    its FP32 shadow, written wherever a column of V is written; the
+//          CGS update reads it for the columns whose coefficient is so small
+//          that FP32 products keep the update FP64-accurate (k_apply),
 //   r0/r1  residual ping-pong (step j reads r[j&1], writes r[(j+1)&1]),
 //   small  the ncv-sized arrays of the reference's workl (T, Ritz values,
 //          bounds, Q), see the SM_* offsets,
@@ -40,16 +43,22 @@ struct State {
     int need2, need3;      // DGKS second / third pass needed for the current step
     int max_iter;
     int nev0, np0, ncv;
-    int err;               // device-detected inconsistency (never expected)
+    int err;               // DEV_ERR_*: a bounded device wait gave up (the solve is abandoned)
     double rnorm, wnorm;
     double tol, eps23;
     long long spmv, passes;
     long long sumc;        // sum over CGS passes of the column count c (algorithmic bytes)
     long long sumnev;      // sum over applied restarts of nev (algorithmic bytes)
+    long long sumt;        // sum over CGS updates of the columns read from the FP32 shadow
     int napply;            // restarts applied to V
     int fin;               // 0 = not finalised, 1 = Qfull/values ready, 2 = Ritz vectors written
-    int pad1;
+    int wait_limit;        // polls of a bounded device wait (0: WAIT_LIMIT_DEFAULT, < 0: none)
 };
+
+// Error codes a kernel leaves in State::err (the host returns them as
+// HLANC_ERR_DEVICE_TIMEOUT).
+enum : int { DEV_ERR_NONE = 0, DEV_ERR_MMA_WAIT = 1 };
+constexpr int WAIT_LIMIT_DEFAULT = 1 << 20;   // far above any real wait
 
 // offsets (in doubles) of the per-problem small arrays, m = ncv
 __host__ __device__ inline int SM_H(int)        { return 0; }           // h[j]=beta_j, h[m+j]=alpha_j
@@ -76,6 +85,7 @@ struct Problem {
     int fp32;              // SpMV on FP32 values/vectors
     int pstride;           // values per tile partial slot (part is pstride x ntiles, value-major)
     double *V;
+    float *V32;            // FP32 shadow of V (same layout), read by the CGS update (k_apply)
     double *r0, *r1;
     double *part;          // tile partial sums, value-major (pstride x ntiles)
     double *gpart;         // group partial sums, value-major (pstride x ngroups)
@@ -286,13 +296,16 @@ void prof_end(int cls, cudaStream_t s);
 void launch_start_vector(const Problem *P_d, const Tile *tiles_d, int ntiles, int prob,
                          unsigned long long seed, cudaStream_t s);
 void launch_norm_init(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s);
+// cgs_flags: CGS_PROJ_HYBRID (hybrid projection panels), CGS_APPLY_SHADOW
+// (update reads the FP32 shadow for small coefficients)
+enum : int { CGS_PROJ_HYBRID = 1, CGS_APPLY_SHADOW = 2 };
 void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const SpmvTile *stiles_d,
-                 int nstiles, int step, bool fp32_any, bool external_w, bool cgs_hybrid, const Problem *one,
+                 int nstiles, int step, bool fp32_any, bool external_w, int cgs_flags, const Problem *one,
                  int one_tr, cudaStream_t s);
 void launch_prep_f32(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, cudaStream_t s);
 void launch_diag_fill(double *x, size_t count, double scale, unsigned long long key, cudaStream_t s);
 void launch_cgs_kernel(const Problem *P_d, const Tile *tiles_d, int ntiles, const Problem *one, int one_tr,
-                       int step, int pass, int which, bool hybrid, cudaStream_t s);
+                       int step, int pass, int which, bool variant, cudaStream_t s);
 void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int step, double *xout,
                      cudaStream_t s);
 void launch_restart(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
@@ -316,8 +329,10 @@ void launch_residuals(const int *row_ptr, const int *col, const double *val, int
                       const double *values_d, const double *vectors_d, int ldv, double *out4k,
                       cudaStream_t s);
 
-// Kernels this library launched (all host threads).
+// Kernels this library launched (all host threads), and launches per
+// kernel variant (HLANC_KL_*).
 std::atomic<long long> &launch_counter();
+std::atomic<long long> &variant_counter(int kind);
 
 // Read-only view of a device CSR operator's arrays (engine.cu).
 struct CsrView {

@@ -389,9 +389,13 @@ __global__ void __launch_bounds__(TPB) k_basis(const Problem *__restrict__ probs
                 if (i >= i0 && i < nev) acc[i] = fma(v, qk[i], acc[i]);
             accn = fma(v, qk[MAXOUT], accn);
         }
+        float *vr32 = P.V32 + r;
 #pragma unroll
         for (int i = 0; i < MAXOUT; ++i)
-            if (i < nev) vr[(size_t)i * ld] = acc[i];
+            if (i < nev) {
+                vr[(size_t)i * ld] = acc[i];
+                vr32[(size_t)i * ld] = (float)acc[i];
+            }
         double res = rin[r] * qlast;                // HLanc.hpp:1605-1614
         if (hn > 0.0) res = res + hn * accn;
         rout[r] = res;
@@ -444,6 +448,7 @@ __global__ void __launch_bounds__(WIDE_TPB) k_basis_wide(const Problem *__restri
             double acc = 0.0;
             for (int k = 0; k < k1; ++k) acc = fma(my[k], qi[k], acc);
             vr[(size_t)i * ld] = acc;
+            P.V32[r + (size_t)i * ld] = (float)acc;
         }
         const double *qn = Q + (size_t)nev * m;
         double accn = 0.0;
@@ -731,6 +736,7 @@ void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_n
         k_basis_wide<<<ntiles, WIDE_TPB, smem, s>>>(P_d, tiles_d);
         prof_end(KC_BASIS, s);
         launch_counter() += 1;
+        variant_counter(HLANC_KL_BASIS_FP64) += 1;
         return;
     }
     switch ((max_nev + 3) / 4) {
@@ -749,6 +755,7 @@ void launch_basis(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_n
     default: basis_t<64>(P_d, tiles_d, ntiles, max_ncv, s); break;
     }
     launch_counter() += 1;
+    variant_counter(HLANC_KL_BASIS_FP64) += 1;
 }
 
 void launch_finalize(const Problem *P_d, int nprob, int, cudaStream_t s) {

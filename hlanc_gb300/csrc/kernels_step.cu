@@ -29,6 +29,11 @@ std::atomic<long long> &launch_counter() {
     return c;
 }
 
+std::atomic<long long> &variant_counter(int kind) {
+    static std::atomic<long long> c[HLANC_KL_KINDS];
+    return c[(kind > 0 && kind < HLANC_KL_KINDS) ? kind : 0];
+}
+
 // ---- SplitMix64 start vector (same formula as generators.start_vector) ----
 __host__ __device__ inline uint64_t sm_mix(uint64_t z) {
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
@@ -198,6 +203,7 @@ __global__ void __launch_bounds__(TPB, F32 ? 5 : SPMV_CTAS_PER_SM) k_spmv_step(c
     const double *__restrict__ rin = step_in(P, j);
     double *__restrict__ w = step_out(P, j);
     double *__restrict__ vj = P.V + (size_t)j * P.ld;
+    float *__restrict__ vj32 = P.V32 + (size_t)j * P.ld;
     if constexpr (F32) {
         spmv_unit<float>(t, P.row_ptr, P.col, P.val32, P.x32, s_col, s_val, red,
                          [=](int rr, float acc) { w[rr] = (double)acc; });
@@ -206,8 +212,10 @@ __global__ void __launch_bounds__(TPB, F32 ? 5 : SPMV_CTAS_PER_SM) k_spmv_step(c
         // in a separate pass over the unit's rows before the gathers start
         spmv_unit<double>(t, P.row_ptr, P.col, P.val, rin, s_col, s_val, red, [=](int rr, double acc) {
             const double x = rin[rr];
+            const double v = scale ? x * t1 : x;
             w[rr] = scale ? acc * t1 : acc;
-            vj[rr] = scale ? x * t1 : x;
+            vj[rr] = v;
+            vj32[rr] = (float)v;
         });
     }
     pdl_trigger();
@@ -229,10 +237,12 @@ __global__ void __launch_bounds__(TPB) k_prep(const Problem *__restrict__ probs,
     const double t1 = scale ? 1.0 / rn : 1.0;
     const double *__restrict__ rin = step_in(P, j);
     double *__restrict__ vj = P.V + (size_t)j * P.ld;
+    float *__restrict__ vj32 = P.V32 + (size_t)j * P.ld;
     for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
         const double x = rin[r];
         const double v = scale ? x * t1 : x;
         vj[r] = v;
+        vj32[r] = (float)v;
         if (ext) xout[r] = v;
         else P.x32[r] = (float)v;
     }
@@ -466,71 +476,84 @@ __global__ void __launch_bounds__(TPB, 4) k_proj(const Problem *__restrict__ pro
 }
 
 // ---- CGS update: w -= V[:, 0:c) h ; DGKS decision ------------------------------
-// The hybrid kernel (HY) runs about half of the columns (whole groups of 8)
-// as FP64 FMAs and the rest as exact fixed-point products (h scaled by its
-// largest entry); the integer sum of a row is converted once and subtracted.
-// Measured on GB300 (n = 4.1M, 32 columns): 186 us against 245 us for the
-// all-FP64 loop; interleaving 4 + 4 columns inside every group of 8 was no
-// faster than all-FP64 in the solver.
-// The last R < 8 columns of an update row, unrolled so that their loads
-// are issued together: FP64 FMAs, or exact integer products.
+// SHADOW (the default update): a column whose coefficient is tiny next to
+// the norm s of the vector being updated, |h_i| <= 2^-32 s / c, is read from
+// the FP32 shadow V32 and accumulated in FP32; the other columns read V and
+// accumulate in FP64.  In a Lanczos step only v_j and v_{j-1} carry large
+// coefficients (alpha_j, beta_j) on the first pass; the older columns' are
+// at the level of the basis' loss of orthogonality, and on the second pass
+// every coefficient is.  The FP32 terms' error, relative (c + 3) 2^-24 each,
+// sums to at most (c + 3) 2^-56 s: the FP64 rounding level of the update
+// (the reference's FP64 gemv has a worst case of c 2^-53 |V||h|).  So the
+// update keeps FP64 accuracy while most columns move 4 bytes per element
+// instead of 8, and only the FP64 columns use the (slow on GB300) FP64 pipe.
+// s is ||w|| on the first pass (from the projection) and the norm left by
+// the previous update on later passes; the FP32 coefficients are scaled by
+// 2^-ilogb(s) so no value approaches FP32's range limits.  A non-finite or
+// zero s sends every column to FP64.  Without SHADOW (HLANC_CGS_FP64) every
+// column is an FP64 FMA.
+// The last R < 8 columns of an update, for two consecutive rows, unrolled
+// so that their loads are issued together.
 template <int R>
-__device__ __forceinline__ double apply_tail_fp64(const double *__restrict__ vr, size_t ld, int k,
-                                                  const double *hs, double acc) {
-    double v[R > 0 ? R : 1];
+__device__ __forceinline__ void apply_tail_fp64(const double *__restrict__ vr, size_t ld, int k,
+                                                const double *hs, double2 &acc) {
+    double2 v[R > 0 ? R : 1];
 #pragma unroll
-    for (int q = 0; q < R; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
-#pragma unroll
-    for (int q = 0; q < R; ++q) acc = fma(-v[q], hs[k + q], acc);
-    return acc;
-}
-
-template <int R>
-__device__ __forceinline__ void apply_tail_int(const double *__restrict__ vr, size_t ld, int k, const int *h1s,
-                                               const int *h0s, FxAcc &A) {
-    double v[R > 0 ? R : 1];
-#pragma unroll
-    for (int q = 0; q < R; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
+    for (int q = 0; q < R; ++q) v[q] = __ldcs(reinterpret_cast<const double2 *>(vr + (size_t)(k + q) * ld));
 #pragma unroll
     for (int q = 0; q < R; ++q) {
-        int x1, x0;
-        fx_split(v[q], FX_RS_UNIT, x1, x0);
-        fx_mac(A, x1, x0, h1s[k + q], h0s[k + q]);
+        acc.x = fma(-v[q].x, hs[k + q], acc.x);
+        acc.y = fma(-v[q].y, hs[k + q], acc.y);
     }
 }
 
-__device__ __forceinline__ double apply_tail_fp64_n(const double *__restrict__ vr, size_t ld, int k, int r,
-                                                    const double *hs, double acc) {
+__device__ __forceinline__ void apply_tail_fp64_n(const double *__restrict__ vr, size_t ld, int k, int r,
+                                                  const double *hs, double2 &acc) {
     switch (r) {
-    case 1: return apply_tail_fp64<1>(vr, ld, k, hs, acc);
-    case 2: return apply_tail_fp64<2>(vr, ld, k, hs, acc);
-    case 3: return apply_tail_fp64<3>(vr, ld, k, hs, acc);
-    case 4: return apply_tail_fp64<4>(vr, ld, k, hs, acc);
-    case 5: return apply_tail_fp64<5>(vr, ld, k, hs, acc);
-    case 6: return apply_tail_fp64<6>(vr, ld, k, hs, acc);
-    case 7: return apply_tail_fp64<7>(vr, ld, k, hs, acc);
-    default: return acc;
-    }
-}
-
-__device__ __forceinline__ void apply_tail_int_n(const double *__restrict__ vr, size_t ld, int k, int r,
-                                                 const int *h1s, const int *h0s, FxAcc &A) {
-    switch (r) {
-    case 1: apply_tail_int<1>(vr, ld, k, h1s, h0s, A); break;
-    case 2: apply_tail_int<2>(vr, ld, k, h1s, h0s, A); break;
-    case 3: apply_tail_int<3>(vr, ld, k, h1s, h0s, A); break;
-    case 4: apply_tail_int<4>(vr, ld, k, h1s, h0s, A); break;
-    case 5: apply_tail_int<5>(vr, ld, k, h1s, h0s, A); break;
-    case 6: apply_tail_int<6>(vr, ld, k, h1s, h0s, A); break;
-    case 7: apply_tail_int<7>(vr, ld, k, h1s, h0s, A); break;
+    case 1: apply_tail_fp64<1>(vr, ld, k, hs, acc); break;
+    case 2: apply_tail_fp64<2>(vr, ld, k, hs, acc); break;
+    case 3: apply_tail_fp64<3>(vr, ld, k, hs, acc); break;
+    case 4: apply_tail_fp64<4>(vr, ld, k, hs, acc); break;
+    case 5: apply_tail_fp64<5>(vr, ld, k, hs, acc); break;
+    case 6: apply_tail_fp64<6>(vr, ld, k, hs, acc); break;
+    case 7: apply_tail_fp64<7>(vr, ld, k, hs, acc); break;
     default: break;
     }
 }
 
-template <bool HY, bool ONE>
-__global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__restrict__ probs,
-                                               const Tile *__restrict__ tiles, const Problem P1, int tr,
-                                               int s, int pass) {
+template <int R>
+__device__ __forceinline__ void apply_tail_f32(const float *__restrict__ vr, size_t ld, int k, const float *hs,
+                                               float2 &acc) {
+    float2 v[R > 0 ? R : 1];
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = __ldcs(reinterpret_cast<const float2 *>(vr + (size_t)(k + q) * ld));
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        acc.x = fmaf(v[q].x, hs[k + q], acc.x);
+        acc.y = fmaf(v[q].y, hs[k + q], acc.y);
+    }
+}
+
+__device__ __forceinline__ void apply_tail_f32_n(const float *__restrict__ vr, size_t ld, int k, int r,
+                                                 const float *hs, float2 &acc) {
+    switch (r) {
+    case 1: apply_tail_f32<1>(vr, ld, k, hs, acc); break;
+    case 2: apply_tail_f32<2>(vr, ld, k, hs, acc); break;
+    case 3: apply_tail_f32<3>(vr, ld, k, hs, acc); break;
+    case 4: apply_tail_f32<4>(vr, ld, k, hs, acc); break;
+    case 5: apply_tail_f32<5>(vr, ld, k, hs, acc); break;
+    case 6: apply_tail_f32<6>(vr, ld, k, hs, acc); break;
+    case 7: apply_tail_f32<7>(vr, ld, k, hs, acc); break;
+    default: break;
+    }
+}
+
+// Six CTAs per SM for single-problem launches (40 registers); the batched
+// form's table loads need a few more registers, so it runs five.
+template <bool SHADOW, bool ONE>
+__global__ void __launch_bounds__(TPB, ONE ? 6 : 5) k_apply(const Problem *__restrict__ probs,
+                                                  const Tile *__restrict__ tiles, const Problem P1, int tr,
+                                                  int s, int pass) {
     pdl_wait();
     const TileRows<ONE> t(tiles, P1, tr);
     const Problem &P = ONE ? P1 : probs[t.prob];
@@ -542,79 +565,70 @@ __global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__rest
     const int m = P.ncv;
     double *__restrict__ w = step_out(P, j);
     __shared__ double hs[MAXNCV];
-    __shared__ int h1s[MAXNCV], h0s[MAXNCV];
+    __shared__ float h32s[MAXNCV];
     __shared__ double scratch[32], mine[1], tot[1];
-    __shared__ int s_zero;
-    __shared__ unsigned s_hmax;
+    __shared__ int s_zero, s_t;
     const double *hv = P.small + SM_HV(m);
-    if (threadIdx.x == 0) s_hmax = 0u;
+    // norm of the vector this pass updates (HLanc.hpp:1429 / 1440-1458)
+    const double sc = pass == 1 ? S->wnorm : S->rnorm;
+    const bool usable = SHADOW && sc > 0.0 && sc <= DBL_MAX;
+    const double thr = usable ? ldexp(sc, -32) / c : 0.0;
+    if (threadIdx.x == 0) s_t = usable ? c : 0;
     __syncthreads();
     for (int i = threadIdx.x; i < c; i += TPB) {
-        hs[i] = hv[i];
-        if (HY) atomicMax(&s_hmax, fx_hi_abs(hv[i]));
+        const double h = hv[i];
+        hs[i] = h;
+        if (usable && !(fabs(h) <= thr)) atomicMin(&s_t, i);
     }
     __syncthreads();
-    const int eh = fx_scale(s_hmax);
-    if (HY)
-        for (int i = threadIdx.x; i < c; i += TPB) fx_split(hs[i], 1027 + eh, h1s[i], h0s[i]);
+    const int tf = s_t;                       // columns [0, tf) in FP32, [tf, c) in FP64
+    const int ke = usable ? -ilogb(sc) : 0;
+    for (int i = threadIdx.x; i < tf; i += TPB) h32s[i] = (float)ldexp(hs[i], ke);
     __syncthreads();
+    const double unscale = ldexp(1.0, -ke);
     const size_t ld = (size_t)P.ld;
-    // FP64 share: whole groups of 8, about half of the columns (all below 8)
-    const int cd = c < 8 ? c : ((c + 8) >> 4) << 3;
     double nrm = 0.0;
-    for (int r = t.row0 + threadIdx.x; r < t.row1; r += TPB) {
-        const double *__restrict__ vr = P.V + r;
-        double acc = w[r];
+    // Two consecutive rows per thread (8-byte FP32 / 16-byte FP64 loads):
+    // twice the bytes in flight per load.  Tiles start on 64-row boundaries;
+    // an odd last row n - 1 is paired with padding row n (< ld), whose w and
+    // V entries are zero and stay zero, so it adds nothing.
+    const int rend = min(P.ld, (t.row1 + 1) & ~1);
+    for (int r = t.row0 + 2 * (int)threadIdx.x; r < rend; r += 2 * TPB) {
+        double2 acc = *reinterpret_cast<const double2 *>(w + r);
         int k = 0;
-        if constexpr (HY) {
-            // columns [0, cd) as FP64 FMAs, [cd, c) as exact integer products
-            for (; k + 8 <= cd; k += 8) {
-                double v[8];
+        if (SHADOW && tf > 0) {
+            const float *__restrict__ vr32 = P.V32 + r;
+            float2 a32 = make_float2(0.0f, 0.0f);
+            for (; k + 8 <= tf; k += 8) {
+                float2 v[8];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
+                for (int q = 0; q < 8; ++q) v[q] = __ldcs(reinterpret_cast<const float2 *>(vr32 + (size_t)(k + q) * ld));
 #pragma unroll
-                for (int q = 0; q < 8; ++q) acc = fma(-v[q], hs[k + q], acc);
-            }
-            if (k < cd) {           // only when c < 8 (cd = c)
-                acc = apply_tail_fp64_n(vr, ld, k, cd - k, hs, acc);
-                k = cd;
-            }
-            if (k < c) {
-                FxAcc A;
-                fx_zero(A);
-                int steps = 0;
-                for (; k + 8 <= c; k += 8) {
-                    double v[8];
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        int x1, x0;
-                        fx_split(v[q], FX_RS_UNIT, x1, x0);
-                        fx_mac(A, x1, x0, h1s[k + q], h0s[k + q]);
-                    }
-                    steps += 8;
-                    if (steps == FX_MACS) {
-                        steps = 0;
-                        fx_carry(A);
-                    }
+                for (int q = 0; q < 8; ++q) {
+                    a32.x = fmaf(v[q].x, h32s[k + q], a32.x);
+                    a32.y = fmaf(v[q].y, h32s[k + q], a32.y);
                 }
-                // at most 7 more steps after 0 or 8: within the carry budget
-                apply_tail_int_n(vr, ld, k, c - k, h1s, h0s, A);
-                acc -= fx_to_double(A, eh - 114);
             }
-        } else {
-            for (; k + 8 <= c; k += 8) {
-                double v[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) v[q] = __ldcs(vr + (size_t)(k + q) * ld);
-#pragma unroll
-                for (int q = 0; q < 8; ++q) acc = fma(-v[q], hs[k + q], acc);
-            }
-            acc = apply_tail_fp64_n(vr, ld, k, c - k, hs, acc);
+            apply_tail_f32_n(vr32, ld, k, tf - k, h32s, a32);
+            k = tf;
+            acc.x = fma(-(double)a32.x, unscale, acc.x);
+            acc.y = fma(-(double)a32.y, unscale, acc.y);
         }
-        w[r] = acc;
-        nrm = fma(acc, acc, nrm);
+        const double *__restrict__ vr = P.V + r;
+        for (; k + 8 <= c; k += 8) {
+            double2 v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = __ldcs(reinterpret_cast<const double2 *>(vr + (size_t)(k + q) * ld));
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                acc.x = fma(-v[q].x, hs[k + q], acc.x);
+                acc.y = fma(-v[q].y, hs[k + q], acc.y);
+            }
+        }
+        apply_tail_fp64_n(vr, ld, k, c - k, hs, acc);
+        *reinterpret_cast<double2 *>(w + r) = acc;
+        nrm = fma(acc.x, acc.x, nrm);
+        nrm = fma(acc.y, acc.y, nrm);
     }
     pdl_trigger();
     nrm = block_sum0(nrm, scratch);
@@ -625,6 +639,7 @@ __global__ void __launch_bounds__(TPB, HY ? 4 : 6) k_apply(const Problem *__rest
         const double nr = sqrt(tot[0]);
         s_zero = 0;
         S->sumc += c;
+        S->sumt += tf;
         if (pass == 1) {                               // HLanc.hpp:1440-1444
             S->rnorm = nr;
             S->need2 = nr < S->wnorm * 0.717;
@@ -750,7 +765,7 @@ void launch_prep_ext(const Problem *P_d, const Tile *tiles_d, int ntiles, int st
 // One Lanczos step for every active problem of the tile table.  With
 // external_w the operator output was already written by the host path.
 void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const SpmvTile *stiles_d,
-                 int nstiles, int step, bool fp32_any, bool external_w, bool cgs_hybrid, const Problem *one,
+                 int nstiles, int step, bool fp32_any, bool external_w, int cgs_flags, const Problem *one,
                  int one_tr, cudaStream_t s) {
     if (!external_w) {
         if (fp32_any) {
@@ -769,10 +784,10 @@ void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const Spmv
     }
     for (int pass = 1; pass <= 3; ++pass) {
         prof_begin(s);
-        launch_cgs_kernel(P_d, tiles_d, ntiles, one, one_tr, step, pass, 0, cgs_hybrid, s);
+        launch_cgs_kernel(P_d, tiles_d, ntiles, one, one_tr, step, pass, 0, (cgs_flags & CGS_PROJ_HYBRID) != 0, s);
         prof_end(KC_PROJ, s);
         prof_begin(s);
-        launch_cgs_kernel(P_d, tiles_d, ntiles, one, one_tr, step, pass, 1, cgs_hybrid, s);
+        launch_cgs_kernel(P_d, tiles_d, ntiles, one, one_tr, step, pass, 1, (cgs_flags & CGS_APPLY_SHADOW) != 0, s);
         prof_end(KC_APPLY, s);
     }
 }
@@ -790,14 +805,17 @@ void launch_diag_fill(double *x, size_t count, double scale, unsigned long long 
     launch_counter() += 1;
 }
 
-// which: 0 = projection, 1 = update.  one: the host copy of the descriptor
-// of a single-problem launch (tiles of one_tr rows), or null.
+// which: 0 = projection (variant: hybrid FP64 + fixed-point panels), 1 =
+// update (variant: FP32 shadow for small coefficients).  one: the host copy
+// of the descriptor of a single-problem launch (tiles of one_tr rows), or null.
 void launch_cgs_kernel(const Problem *P_d, const Tile *tiles_d, int ntiles, const Problem *one, int one_tr,
-                       int step, int pass, int which, bool hybrid, cudaStream_t s) {
+                       int step, int pass, int which, bool variant, cudaStream_t s) {
     Problem P1;
     if (one) P1 = *one;
     else memset(&P1, 0, sizeof P1);
-    const int code = (which << 2) | (hybrid ? 2 : 0) | (one ? 1 : 0);
+    const int code = (which << 2) | (variant ? 2 : 0) | (one ? 1 : 0);
+    variant_counter(which == 0 ? (variant ? HLANC_KL_PROJ_HYBRID : HLANC_KL_PROJ_FP64)
+                               : (variant ? HLANC_KL_APPLY_SHADOW : HLANC_KL_APPLY_FP64)) += 1;
     const dim3 g(ntiles), b(TPB);
     switch (code) {
     case 0: (void)launch_pdl(k_proj<false, false>, g, b, s, P_d, tiles_d, P1, one_tr, step, pass); break;

@@ -51,7 +51,6 @@ constexpr int NDIG = 7;       // digit planes / levels
 constexpr int KMAX = 64;      // largest padded ncv
 constexpr int NMAX = 64;      // largest padded nev + 1
 constexpr int THREADS = 256;
-constexpr unsigned SPIN_LIMIT = 1u << 20;   // MMA completion wait (far above any real wait)
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -260,6 +259,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
     State *S = P.st;
     if (S->status != ST_RUNNING || S->phase != PH_APPLY) return;
     const int m = P.ncv, nev = S->nev, np = S->np;
+    const int wl = S->wait_limit;
+    const unsigned wait_limit = wl == 0 ? (unsigned)WAIT_LIMIT_DEFAULT : (wl < 0 ? 0u : (unsigned)wl);
     const int kpad = (m + 15) & ~15;
     const int nout = nev + 1;
     constexpr uint32_t NCOLS = (NDIG * NPAD > 256) ? 512u : (NDIG * NPAD > 128 ? 256u : 128u);
@@ -391,14 +392,17 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
             }
             mma_commit(&s_mbar);
         }
-        // 4. wait for the products (bounded)
+        // 4. wait for the products (bounded).  A wait that gives up marks the
+        //    CTA failed, then waits (again bounded) for the MMAs it already
+        //    issued, so tensor memory is not released under them.
         {
-            unsigned spins = 0;
-            while (!mbar_try_wait(&s_mbar, phase)) {
-                if (++spins > SPIN_LIMIT) {
-                    s_fail = 1;
-                    break;
-                }
+            bool done = false;
+            for (unsigned spins = 0; spins < wait_limit; ++spins)
+                if (mbar_try_wait(&s_mbar, phase)) { done = true; break; }
+            if (!done) {
+                s_fail = 1;
+                for (unsigned spins = 0; spins < (unsigned)WAIT_LIMIT_DEFAULT; ++spins)
+                    if (mbar_try_wait(&s_mbar, phase)) break;
             }
         }
         phase ^= 1u;
@@ -427,6 +431,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
                     const double v = combine(lv, exr, s_colexp[i]);
                     if (i < nev) {
                         P.V[orow + (size_t)i * ld] = v;
+                        P.V32[orow + (size_t)i * ld] = (float)v;
                     } else {                                      // residual (HLanc.hpp:1605-1614)
                         double res = rin[orow] * qlast;
                         if (hn > 0.0) res = res + hn * v;
@@ -447,10 +452,10 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
         fence_after();
         tmem_dealloc(taddr, NCOLS);
     }
-    if (s_fail) {
-        if (tid == 0) atomicExch(&S->err, 5);
-        return;
-    }
+    // A failed CTA still takes part in the tile reduction below, so the tile
+    // group's counters are reset for the next launch; the host reads S->err
+    // after the cycle and abandons the solve.
+    if (s_fail && tid == 0) atomicExch(&S->err, DEV_ERR_MMA_WAIT);
     nrm = block_sum0(nrm, s_red);
     if (tid == 0) s_mine[0] = nrm;
     __syncthreads();
@@ -477,6 +482,7 @@ static void basis_tc_t(const Problem *P_d, const Tile *tiles_d, int ntiles, cuda
     k_basis_tc<NPAD><<<ntiles, tc::THREADS, smem, s>>>(P_d, tiles_d);
     prof_end(KC_BASIS, s);
     launch_counter() += 1;
+    variant_counter(HLANC_KL_BASIS_TC) += 1;
 }
 
 // The tensor-core basis update serves problems with ncv <= 64 and

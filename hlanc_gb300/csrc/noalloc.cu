@@ -16,8 +16,12 @@
 //
 // Host code cannot use the array's name as a device address (there it is a
 // host-side stand-in), so the first call on each device looks the address up
-// with cudaGetSymbolAddress, with that device current, and caches it; make
-// that first call outside any stream capture.
+// with cudaGetSymbolAddress, with that device current, and caches it with the
+// device's current context; a call that finds a different context (the old
+// one was destroyed, e.g. by cudaDeviceReset, and the module loaded afresh)
+// looks it up again.  Make the first call on a device, and the first after
+// such a reset, outside any stream capture.
+#include <cuda.h>            // CUcontext only; the driver call is found through the runtime
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -25,6 +29,22 @@
 #include "internal.cuh"
 
 namespace {
+
+// cuCtxGetCurrent, looked up once through the runtime (no link against the
+// driver library); null if unavailable, in which case every call looks the
+// scratch address up again.
+typedef CUresult (*ctx_get_fn)(CUcontext *);
+ctx_get_fn ctx_get() {
+    static const ctx_get_fn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return (ctx_get_fn)p;
+    }();
+    return fn;
+}
 
 constexpr int NA_BLOCKS = 256;                       // CTAs per pair
 constexpr int NA_MAX = HLANC_NOALLOC_MAX_PAIRS;      // pairs per call
@@ -36,6 +56,7 @@ static __device__ __align__(256) double g_noalloc_scratch[NA_TOTAL];
 constexpr int NA_MAX_DEVICES = 64;
 std::mutex g_na_mu;
 double *g_na_ptr[NA_MAX_DEVICES] = {nullptr};
+CUcontext g_na_ctx[NA_MAX_DEVICES] = {nullptr};
 
 // Per CTA of pair i: sum of squares of A v - lambda v, max |A v - lambda v|,
 // max |A v|, max |lambda v| over its rows (the quantities of verify_eigs).
@@ -91,19 +112,22 @@ __global__ void k_na_resid_final(int nblk, int k, double *__restrict__ scratch) 
     scratch[NA_PART + NA_MAX + i] = mx > 0.0 ? b / mx : b;
 }
 
-// Device address of the scratch array on `dev` (looked up once per device).
+// Device address of the scratch array on `dev`, which must be current:
+// looked up once per device and context.
 int scratch_for(int dev, double **out) {
     if (dev < 0 || dev >= NA_MAX_DEVICES) return HLANC_ERR_UNSUPPORTED;
     std::lock_guard<std::mutex> lk(g_na_mu);
-    if (!g_na_ptr[dev]) {
-        int prev = -1;
-        if (cudaGetDevice(&prev) != cudaSuccess) return HLANC_ERR_CUDA;
-        if (prev != dev && cudaSetDevice(dev) != cudaSuccess) return HLANC_ERR_CUDA;
+    CUcontext ctx = nullptr;
+    const ctx_get_fn get = ctx_get();
+    if (get && get(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+    if (!g_na_ptr[dev] || !ctx || ctx != g_na_ctx[dev]) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (prev != dev) cudaSetDevice(prev);
         if (e != cudaSuccess || !p) return HLANC_ERR_CUDA;
+        CUcontext now = nullptr;       // the lookup may have created the primary context
+        if (get && get(&now) != CUDA_SUCCESS) now = nullptr;
         g_na_ptr[dev] = static_cast<double *>(p);
+        g_na_ctx[dev] = now;
     }
     *out = g_na_ptr[dev];
     return HLANC_OK;
@@ -115,15 +139,18 @@ extern "C" int hlanc_residuals_device_noalloc(hlanc_csr_t csr, int k, const doub
                                               const double *vectors_d, int ldv_d, double *resid_h,
                                               double *rdiff_h) {
     hlanc::CsrView c;
-    if (!csr || k <= 0 || !values_d || !vectors_d || !resid_h || !rdiff_h) return HLANC_ERR_INVALID;
+    if (!csr || k <= 0 || !values_d || !vectors_d) return HLANC_ERR_INVALID;
     if (hlanc::csr_view_of(csr, &c) != HLANC_OK || ldv_d < c.nrows || c.ncols > c.nrows) return HLANC_ERR_INVALID;
     if (k > NA_MAX) return HLANC_ERR_UNSUPPORTED;   // more pairs than the fixed scratch holds
-    double *scratch = nullptr;
-    int rc = scratch_for(c.dev, &scratch);
-    if (rc) return rc;
     int prev = -1;
     cudaGetDevice(&prev);
     if (prev != c.dev) cudaSetDevice(c.dev);
+    double *scratch = nullptr;
+    int rc = scratch_for(c.dev, &scratch);
+    if (rc) {
+        if (prev != c.dev) cudaSetDevice(prev);
+        return rc;
+    }
     int nblk = (c.nrows + 255) / 256;
     if (nblk > NA_BLOCKS) nblk = NA_BLOCKS;
     if (nblk < 1) nblk = 1;
@@ -132,9 +159,10 @@ extern "C" int hlanc_residuals_device_noalloc(hlanc_csr_t csr, int k, const doub
     k_na_resid_final<<<(k + 127) / 128, 128, 0, c.stream>>>(nblk, k, scratch);
     hlanc::launch_counter() += 2;
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess)
+    // each output is optional, as in hlanc_residuals_device
+    if (e == cudaSuccess && resid_h)
         e = cudaMemcpyAsync(resid_h, scratch + NA_PART, sizeof(double) * k, cudaMemcpyDeviceToHost, c.stream);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && rdiff_h)
         e = cudaMemcpyAsync(rdiff_h, scratch + NA_PART + NA_MAX, sizeof(double) * k, cudaMemcpyDeviceToHost,
                             c.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);

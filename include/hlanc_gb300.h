@@ -43,13 +43,17 @@ extern "C" {
 #define HLANC_BASIS_FP64          1  /* always the FP64 CUDA-core kernel */
 
 /* Arithmetic of the CGS passes h = V^T w, w -= V h (hlanc_opts_t.cgs_kernel).
- * The hybrid kernels run about half of every column panel as FP64 FMAs and
- * the rest as exact fixed-point integer products (inputs quantised to 2^-58
- * of their scale, sums exact), so the FP64 and the integer pipes work at
- * the same time. */
-#define HLANC_CGS_AUTO            0  /* hybrid for launches over >= 2^18 rows, else FP64 */
-#define HLANC_CGS_FP64            1  /* every column as FP64 FMAs */
-#define HLANC_CGS_HYBRID          2  /* hybrid at every size */
+ * The hybrid projection runs 5 of every 8 columns as FP64 FMAs and 3 as
+ * exact fixed-point integer products (inputs quantised to 2^-58 of their
+ * scale, sums exact), so the FP64 and the integer pipes work at the same
+ * time.  The update w -= V h reads an FP32 copy of the basis for every
+ * column whose coefficient is at most 2^-32 ||w|| / c (FP32 products of
+ * such terms stay within the FP64 rounding of the update) and FP64 for the
+ * rest -- in a Lanczos step usually just v_j and v_{j-1}. */
+#define HLANC_CGS_AUTO            0  /* hybrid projection for launches over >= 2^18 rows, else FP64;
+                                        update with the FP32 copy for small coefficients */
+#define HLANC_CGS_FP64            1  /* every column of both passes as FP64 FMAs */
+#define HLANC_CGS_HYBRID          2  /* hybrid projection at every size; update as AUTO */
 
 /* Largest ncv the device restart kernels accept, and largest nev. */
 #define HLANC_MAX_NCV           128
@@ -117,7 +121,10 @@ typedef struct {
     int profile;              /* time every kernel launch with CUDA events (eager launches); see hlanc_last_profile */
     int basis_kernel;         /* HLANC_BASIS_*; default HLANC_BASIS_AUTO */
     int cgs_kernel;           /* HLANC_CGS_*; default HLANC_CGS_AUTO */
-    int reserved[3];
+    int wait_limit;           /* polls of each bounded device wait before it gives up and the
+                                 solve returns HLANC_ERR_DEVICE_TIMEOUT: 0 = default (2^20),
+                                 < 0 = give up at once (tests of the failure path) */
+    int reserved[2];
 } hlanc_opts_t;
 
 /* Fill defaults (tol 0, max_restarts 200, FP64, seed 0, graphs on, host restart). */
@@ -135,7 +142,8 @@ typedef struct {
     double bytes_spmv;        /* algorithmic bytes moved, SpMV */
     double bytes_cgs;         /* algorithmic bytes moved, CGS passes */
     double bytes_restart;     /* algorithmic bytes moved, basis updates + Ritz vectors */
-    double reserved[4];
+    double cgs_update_fp32_share;  /* share of the CGS update's columns read from the FP32 copy */
+    double reserved[3];
 } hlanc_stats_t;
 
 /* ds_solver_gpu(n, nev, ncv, values, vectors, ldv, op, dev): largest
@@ -170,10 +178,11 @@ int hlanc_residuals_device(hlanc_csr_t csr, int k, const double *values_d,
  * cudaMalloc/cudaFree).  Its scratch is a fixed __device__ array of about
  * 513 KB, held by every GPU that loads the library until exit; k may be at
  * most HLANC_NOALLOC_MAX_PAIRS (larger k returns HLANC_ERR_UNSUPPORTED).
- * resid_h / rdiff_h are host arrays of k doubles.  All calls share the
- * scratch, so calls that overlap on the GPU race; serialise them.  The first
- * call on a device looks up the scratch address, so make it outside any
- * stream capture.  Synchronous. */
+ * resid_h / rdiff_h are host arrays of k doubles; either may be NULL, as in
+ * hlanc_residuals_device.  All calls share the scratch, so calls that
+ * overlap on the GPU race; serialise them.  The first call on a device, and
+ * the first after its context was re-created (cudaDeviceReset), looks up the
+ * scratch address, so make those outside any stream capture.  Synchronous. */
 #define HLANC_NOALLOC_MAX_PAIRS 64
 int hlanc_residuals_device_noalloc(hlanc_csr_t csr, int k, const double *values_d,
                                    const double *vectors_d, int ldv_d, double *resid_h,
@@ -248,6 +257,18 @@ int hlanc_server_destroy(hlanc_server_t s);
 /* Number of kernels this library launched since load (all devices). */
 long long hlanc_kernel_launches(void);
 
+/* Launches since load of one kernel variant (no reference counterpart; tests
+ * use it to check which arithmetic a default solve took). */
+#define HLANC_KL_ALL              0  /* every kernel (same as hlanc_kernel_launches) */
+#define HLANC_KL_PROJ_HYBRID      1  /* CGS projection, FP64 + fixed-point panels */
+#define HLANC_KL_PROJ_FP64        2  /* CGS projection, all FP64 */
+#define HLANC_KL_APPLY_SHADOW     3  /* CGS update, FP32 copy for small coefficients */
+#define HLANC_KL_APPLY_FP64       4  /* CGS update, all FP64 */
+#define HLANC_KL_BASIS_TC         5  /* restart basis update on the tensor cores */
+#define HLANC_KL_BASIS_FP64       6  /* restart basis update on FP64 CUDA cores */
+#define HLANC_KL_KINDS            7
+long long hlanc_kernel_launches_of(int kind);
+
 /* Per-kernel-class timing of the last solve run with opts.profile = 1 on the
  * calling thread.  Classes: 0 SpMV, 1 CGS projection, 2 CGS update,
  * 3 basis update (V*Q), 4 Ritz vectors, 5 auxiliary kernels, 6 host restart
@@ -269,7 +290,8 @@ int hlanc_diag_fp64_tflops(int dev, double *tflops);
 /* The CGS kernels alone on a synthetic basis of n rows and c columns
  * (cgs_kernel HLANC_CGS_FP64 or HLANC_CGS_HYBRID), each launched reps times
  * back to back: ms3 = mean ms of a first-pass projection (with ||w||),
- * a second-pass projection and a second-pass update. */
+ * a second-pass projection and a second-pass update (its coefficients at
+ * 1e-13 ||w||, so with HLANC_CGS_HYBRID every column reads the FP32 copy). */
 int hlanc_diag_cgs(int dev, int n, int c, int cgs_kernel, int reps, double *ms3);
 
 #ifdef __cplusplus

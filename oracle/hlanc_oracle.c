@@ -803,6 +803,10 @@ static void householder_apply_right(long n, int m, int k, const double *a, int l
     }
 }
 
+static _Thread_local double *g_trace = NULL;
+static _Thread_local int g_trace_cap = 0;
+void oracle_set_trace(double *buf, int cap) { g_trace = buf; g_trace_cap = buf ? cap : 0; }
+
 /* ds_solver, HLanc.hpp:1650-1850 */
 int oracle_ds_solver(int n, int nev, int ncv, double *values, double *vectors, int ldv,
                      oracle_spmv_fn op, void *op_ctx, const double *start, double tol,
@@ -849,6 +853,9 @@ int oracle_ds_solver(int n, int nev, int ncv, double *values, double *vectors, i
     int iter;
     for (iter = 0; iter < max_iter; ++iter) {                /* H:1684-1736 */
         stats->restarts = iter + 1;
+        const double t_cycle = omp_get_wtime();
+        const long spmv_cycle = stats->spmv_calls;
+        const int k_cycle = nev;
         dsaitr(&s, nev, np, resid, &rnorm, h, ldh, ipj, irj);
         memcpy(ritz, h + ldh, sizeof(double) * (size_t)ncv);
         memcpy(ework, h + 1, sizeof(double) * (size_t)(ncv - 1));
@@ -871,6 +878,14 @@ int oracle_ds_solver(int n, int nev, int ncv, double *values, double *vectors, i
         if (nevbef < nev) dsgets(nev, np, ritz, bounds);
         dsapps(&s, nev, np, ritz, h, ldh, resid, qfull, workd);
         rnorm = dnrm2(n, resid);
+        stats->cycle_seconds = omp_get_wtime() - t_cycle;     /* timing only, no effect on results */
+        stats->cycle_spmv = stats->spmv_calls - spmv_cycle;
+        stats->cycle_k = k_cycle;
+        if (iter < g_trace_cap) {
+            g_trace[3 * iter] = stats->cycle_seconds;
+            g_trace[3 * iter + 1] = (double)stats->cycle_spmv;
+            g_trace[3 * iter + 2] = (double)k_cycle;
+        }
     }
     stats->nconv = nconv;
     stats->rnorm = rnorm;

@@ -67,7 +67,15 @@ typedef struct {
     int  nconv;          /* converged Ritz values at exit                    */
     long cgs_passes;     /* CGS passes (first passes + DGKS corrections)     */
     double rnorm;        /* final residual norm                              */
+    double cycle_seconds;/* wall time of the last restart cycle the loop ran  */
+    long cycle_spmv;     /* its operator applications                        */
+    int cycle_k;         /* its first Lanczos step (the kept columns)        */
 } oracle_stats_t;
+
+/* Optional per-cycle trace of the next solves on this thread (timing
+ * calibration of the CPU baseline): for loop iteration i < cap, buf[3i..3i+2]
+ * = seconds, operator applications, first Lanczos step.  buf = NULL stops. */
+void oracle_set_trace(double *buf, int cap);
 
 /* ds_solver restatement (HLanc.hpp:1650-1850) with mat_v_mkl_t storage
  * (HLanc.hpp:900-948): V lives in `vectors` (ldv >= n, ncv columns).

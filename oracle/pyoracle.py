@@ -28,7 +28,8 @@ class _OCSR(C.Structure):
 
 class _Stats(C.Structure):
     _fields_ = [("spmv_calls", C.c_long), ("restarts", C.c_int), ("nconv", C.c_int),
-                ("cgs_passes", C.c_long), ("rnorm", C.c_double)]
+                ("cgs_passes", C.c_long), ("rnorm", C.c_double), ("cycle_seconds", C.c_double),
+                ("cycle_spmv", C.c_long), ("cycle_k", C.c_int)]
 
 
 def build(force: bool = False) -> str:
@@ -60,6 +61,7 @@ def lib():
                                        _f64p, C.c_double, C.c_int, C.c_int, C.POINTER(_Stats)]
         L.oracle_tridiag_eig.argtypes = [C.c_int, _f64p, _f64p, _f64pF, C.c_int, C.c_int]
         L.oracle_set_threads.argtypes = [C.c_int]
+        L.oracle_set_trace.argtypes = [C.c_void_p, C.c_int]
         _lib = L
     return _lib
 
@@ -114,20 +116,33 @@ def spmv(row_ptr, col, val, ncols, symmetric, x, kind: str = "mkl") -> np.ndarra
 
 
 def solve_csr(row_ptr, col, val, ncols, symmetric, nev, ncv, start, tol=0.0, max_iter=0,
-              threads=1, ldv=None):
-    """Run the oracle ds_solver.  Returns (rc, values[ncv], vectors (ldv x ncv), stats)."""
+              threads=1, ldv=None, trace=False):
+    """Run the oracle ds_solver.  Returns (rc, values[ncv], vectors (ldv x ncv), stats).
+    stats['cycle_*'] describe the last restart cycle; with trace=True,
+    stats['trace'] lists (seconds, operator applications, first step) per cycle."""
     n = len(row_ptr) - 1
     ldv = n if ldv is None else ldv
     m = _to_ocsr(row_ptr, col, val, ncols, symmetric)
     values = np.zeros(ncv)
     vectors = np.zeros((ldv, ncv), order="F")
     st = _Stats()
-    rc = lib().oracle_solve_csr(C.byref(m), nev, ncv, values, vectors, ldv,
-                                np.ascontiguousarray(start, dtype=np.float64), float(tol),
-                                int(max_iter), int(threads), C.byref(st))
+    cap = (max_iter if max_iter > 0 else 200) + 1
+    buf = np.zeros(3 * cap) if trace else None
+    if trace:
+        lib().oracle_set_trace(buf.ctypes.data, cap)
+    try:
+        rc = lib().oracle_solve_csr(C.byref(m), nev, ncv, values, vectors, ldv,
+                                    np.ascontiguousarray(start, dtype=np.float64), float(tol),
+                                    int(max_iter), int(threads), C.byref(st))
+    finally:
+        if trace:
+            lib().oracle_set_trace(None, 0)
     lib().ocsr_free(C.byref(m))
     stats = dict(spmv_calls=st.spmv_calls, restarts=st.restarts, nconv=st.nconv,
-                 cgs_passes=st.cgs_passes, rnorm=st.rnorm)
+                 cgs_passes=st.cgs_passes, rnorm=st.rnorm, cycle_seconds=st.cycle_seconds,
+                 cycle_spmv=st.cycle_spmv, cycle_k=st.cycle_k)
+    if trace:
+        stats["trace"] = buf.reshape(cap, 3)[:st.restarts].tolist()
     return rc, values, vectors, stats
 
 

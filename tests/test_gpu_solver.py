@@ -407,10 +407,14 @@ def test_largest_nev_tensor_core_basis(H):
     op = H.dcsrmv_operator_gpu(m)
     nev = H.HLANC_MAX_NEV
     ref = np.sort(np.linalg.eigvalsh(G.to_scipy(m).toarray()))[-nev:]
+    before = H.variant_counts()
     rc, v, x, st = H.solve(op, nev, 64, tol=1e-10)
+    used = {k: c - before[k] for k, c in H.variant_counts().items()}
     assert rc == 0, st
     assert np.abs(v[:nev] - ref).max() <= EV_RTOL * np.abs(ref).max()
     _check_pairs(m, v, x, nev)
+    # the restarts took the tensor-core update at 64 outputs, never the FP64 kernel
+    assert st["restarts"] > 0 and used["basis_tc"] > 0 and used["basis_fp64"] == 0, used
 
 
 def test_cgs_kernels_alone(H):

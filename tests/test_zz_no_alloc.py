@@ -51,6 +51,11 @@ def test_noalloc_residuals_match_the_allocating_entry_point():
         assert np.allclose(res, ref_res, rtol=1e-12, atol=0.0), (res, ref_res)
         assert np.allclose(rd, ref_rd, rtol=1e-12, atol=0.0), (rd, ref_rd)
     assert res.min() > 0.1          # the second call did not return the first call's residuals
+    # either output may be left out, as with the allocating entry point
+    only = np.full(5, np.nan)
+    assert noalloc(op.handle, 5, shifted.data_ptr(), vecs.data_ptr(), m.n, only.ctypes.data, None) == 0
+    assert np.allclose(only, res, rtol=1e-12, atol=0.0)
+    assert noalloc(op.handle, 5, shifted.data_ptr(), vecs.data_ptr(), m.n, None, rd.ctypes.data) == 0
     # more pairs than the fixed scratch holds: a clear error, not a fault
     big = np.zeros(65)
     assert noalloc(op.handle, 65, vals.data_ptr(), vecs.data_ptr(), m.n, big.ctypes.data, big.ctypes.data) == 7
