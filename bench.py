@@ -54,6 +54,22 @@ sys.path.insert(0, ROOT)
 
 from hlanc_gb300 import generators as G  # noqa: E402
 
+WORKLOADS = {
+    "lap3d_160": dict(desc="3-D Laplacian 160^3 + U[0,0.1) diagonal shift (seed 1)",
+                      gen=lambda: G.laplacian_3d(160, shift_seed=1), nev=20, ncv=60, tol=1e-10),
+    "lap3d_100": dict(desc="3-D Laplacian 100^3 + U[0,0.1) diagonal shift (seed 1)",
+                      gen=lambda: G.laplacian_3d(100, shift_seed=1), nev=20, ncv=60, tol=1e-10),
+    "lap3d_64": dict(desc="3-D Laplacian 64^3 + U[0,0.1) diagonal shift (seed 1)",
+                     gen=lambda: G.laplacian_3d(64, shift_seed=1), nev=20, ncv=60, tol=1e-10),
+    "lap2d_100": dict(desc="2-D Laplacian 100^2 (reference tolerance dlamch('E'))",
+                      gen=lambda: G.laplacian_2d(100), nev=10, ncv=30, tol=0.0),
+    "chunglu_22": dict(desc="normalised adjacency of a Chung-Lu graph, n = 2^22, exponent 2.5, mean degree 32 "
+                            "(seed 2); FP32 SpMV + FP64 refinement",
+                       gen=lambda: G.chung_lu_normalized(1 << 22, seed=2), nev=16, ncv=48, tol=1e-10, mixed=True),
+    "chunglu_22_fp64": dict(desc="normalised adjacency of a Chung-Lu graph, n = 2^22 (seed 2); plain FP64",
+                            gen=lambda: G.chung_lu_normalized(1 << 22, seed=2), nev=16, ncv=48, tol=1e-10),
+}
+
 # Reference fixture of each workload (tests/golden/<name>.npz, written from
 # the reference's own CPU solver): eigenvalues for the parity check and the
 # operator-application count of its full solve (the CPU extrapolation).
@@ -706,7 +722,7 @@ def main():
     # roofline: one profiled solve
     pst = solve_dev(profile=True)
     prof = H.last_profile()
-    kernel_classes = ["spmv", "cgs_proj", "cgs_apply", "basis", "ritz"]
+    kernel_classes = ["spmv", "cgs_proj", "cgs_apply", "basis", "ritz", "cycle"]
     dom = max(kernel_classes, key=lambda k: prof[k]["ms"])
     total_kernel_ms = sum(prof[k]["ms"] for k in kernel_classes + ["aux"])
     peak, peak_src = measured_peaks()

@@ -35,7 +35,9 @@ CGS_HYBRID_MIN_ROWS = 1 << 18     # HLANC_CGS_AUTO picks the hybrid kernels from
 HLANC_MAX_NCV = 128
 HLANC_MAX_NEV = 63
 # kernel variants counted by hlanc_kernel_launches_of
-KL_ALL, KL_PROJ_HYBRID, KL_PROJ_FP64, KL_APPLY_SHADOW, KL_APPLY_FP64, KL_BASIS_TC, KL_BASIS_FP64 = range(7)
+KL_ALL, KL_PROJ_HYBRID, KL_PROJ_FP64, KL_APPLY_SHADOW, KL_APPLY_FP64, KL_BASIS_TC, KL_BASIS_FP64, KL_CYCLE = range(8)
+HLANC_CYCLE_AUTO = 0
+HLANC_CYCLE_OFF = 1
 
 _lib = None
 
@@ -52,7 +54,7 @@ class Opts(C.Structure):
                 ("seed", C.c_ulonglong), ("start", C.POINTER(C.c_double)), ("stream", C.c_void_p),
                 ("use_graphs", C.c_int), ("restart_on_device", C.c_int), ("profile", C.c_int),
                 ("basis_kernel", C.c_int), ("cgs_kernel", C.c_int), ("wait_limit", C.c_int),
-                ("reserved", C.c_int * 2)]
+                ("cycle_kernel", C.c_int), ("reserved", C.c_int * 1)]
 
 
 class Stats(C.Structure):
@@ -66,12 +68,12 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
-PROF_CLASSES = ("spmv", "cgs_proj", "cgs_apply", "basis", "ritz", "aux", "host_restart")
+PROF_CLASSES = ("spmv", "cgs_proj", "cgs_apply", "basis", "ritz", "aux", "host_restart", "cycle")
 
 
 class Profile(C.Structure):
-    _fields_ = [("launches", C.c_longlong * 7), ("ms", C.c_double * 7), ("bytes", C.c_double * 7),
-                ("flops", C.c_double * 7)]
+    _fields_ = [("launches", C.c_longlong * 8), ("ms", C.c_double * 8), ("bytes", C.c_double * 8),
+                ("flops", C.c_double * 8)]
 
     def as_dict(self) -> dict:
         return {name: dict(launches=self.launches[i], ms=self.ms[i], bytes=self.bytes[i], flops=self.flops[i])
@@ -166,12 +168,13 @@ def _check(rc: int, what: str) -> None:
 def opts(tol: float = 0.0, max_restarts: int = 200, precision: int = HLANC_PREC_FP64, seed: int = 0,
          start: Optional[np.ndarray] = None, stream: int = 0, use_graphs: bool = True,
          restart_on_device: bool = False, profile: bool = False, basis_fp64: bool = False,
-         cgs: int = HLANC_CGS_AUTO, wait_limit: int = 0):
+         cgs: int = HLANC_CGS_AUTO, wait_limit: int = 0, cycle: int = 0):
     o = Opts()
     lib().hlanc_opts_default(C.byref(o))
     o.basis_kernel = HLANC_BASIS_FP64 if basis_fp64 else HLANC_BASIS_AUTO
     o.cgs_kernel = cgs
     o.wait_limit = wait_limit
+    o.cycle_kernel = cycle
     o.tol, o.max_restarts, o.precision, o.seed = tol, max_restarts, precision, seed
     o.use_graphs = int(use_graphs)
     o.restart_on_device = int(restart_on_device)
@@ -422,7 +425,7 @@ def kernel_launches_of(kind: int) -> int:
 
 
 def variant_counts() -> dict:
-    names = ("all", "proj_hybrid", "proj_fp64", "apply_shadow", "apply_fp64", "basis_tc", "basis_fp64")
+    names = ("all", "proj_hybrid", "proj_fp64", "apply_shadow", "apply_fp64", "basis_tc", "basis_fp64", "cycle")
     return {nm: kernel_launches_of(i) for i, nm in enumerate(names)}
 
 

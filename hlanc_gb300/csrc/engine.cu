@@ -58,6 +58,7 @@ struct hlanc_csr_s {
     double *xs_d = nullptr, *ys_d = nullptr;   // staging for host vectors (HLanc.hpp:541-549)
     cudaStream_t stream = nullptr;
     double norm_inf = 0.0;                      // max_r sum |a_rc|
+    long long max_row = 0;                      // longest row (entries), general CSR
     std::vector<SpmvTile> stiles_h;             // entry-balanced SpMV work units (prob = 0)
     SpmvTile *stiles_d = nullptr;
     std::mutex mu;
@@ -314,6 +315,11 @@ public:
     int min_tile_rows = 128;
     bool basis_tc = true;                // basis update on the tensor cores when the shape fits
     int cgs_mode = HLANC_CGS_AUTO;       // CGS panels split between the FP64 and the integer pipes
+    int cycle_mode = HLANC_CYCLE_AUTO;   // whole extensions in one cooperative launch when eligible
+    // one-launch extensions (kernels_cycle.cu): CTA table, barrier counters
+    CycTileH *C_d = nullptr;
+    unsigned *bars_d = nullptr;
+    int nctas = 0, nctas_cap = 0;
     long long rows_active = 0;           // rows of all problems in the launch tables
     Problem one_h;                       // descriptor of a single-problem launch table
     int one_tr = 0;                      // its tile rows (0: several problems)
@@ -345,6 +351,8 @@ public:
         if (P_d) cudaFree(P_d);
         if (T_d) cudaFree(T_d);
         if (S_d) cudaFree(S_d);
+        if (C_d) cudaFree(C_d);
+        if (bars_d) cudaFree(bars_d);
         if (off_d) cudaFree(off_d);
         if (flag_d) cudaFree(flag_d);
         if (mbox_d) cudaFree(mbox_d);
@@ -400,6 +408,70 @@ public:
     int cgs_flags() const {
         const bool hy = cgs_mode == HLANC_CGS_HYBRID || (cgs_mode == HLANC_CGS_AUTO && rows_active >= CGS_HYBRID_MIN_ROWS);
         return (hy ? CGS_PROJ_HYBRID : 0) | (cgs_mode != HLANC_CGS_FP64 ? CGS_APPLY_SHADOW : 0);
+    }
+
+    // Problems whose whole extension runs in one cooperative launch: every
+    // active problem has a device operator with rows of at most LONG_ROW
+    // entries (thread-per-row SpMV), and together they have few enough rows
+    // that the per-phase launches are latency-bound.  Each problem gets a
+    // group of CTAs of about cycle_rows_per_cta() rows, no more than its
+    // reduction slots (tiles), and the groups together fit the co-resident
+    // capacity.  Measured on GB300 (whole solves, one launch per extension
+    // against per-phase launches): 2-D Laplacian 10,000 rows 61.7 vs 93.7 ms,
+    // banded 20,000 rows 14.0 vs 24.9 ms, 3-D Laplacian 27,000 rows 60.4 vs
+    // 65.6 ms, but 125,000 rows 204 vs 151 ms; a power-law graph of 16,384
+    // rows (rows up to ~700 entries, one thread each) 91.6 vs 60.8 ms.
+    static constexpr long long CYCLE_MAX_ROWS = 48 * 1024;
+    int rc_cycle = 0;
+    int plan_cycle() {
+        nctas = 0;
+        if (cycle_mode == HLANC_CYCLE_OFF || active.empty() || rows_active > CYCLE_MAX_ROWS) return HLANC_OK;
+        for (int pi : active) {
+            const ProbRes &p = probs[pi];
+            if (!p.csr || p.csr->max_row > LONG_ROW) return HLANC_OK;
+        }
+        static int cap_dev[64] = {0};
+        int d = 0;
+        cudaGetDevice(&d);
+        int cap = (d < 64 && cap_dev[d]) ? cap_dev[d] : cycle_capacity();
+        if (d < 64) cap_dev[d] = cap;
+        if (cap <= 0) return HLANC_OK;
+        const long long per = cycle_rows_per_cta();
+        std::vector<CycTileH> C;
+        for (size_t a = 0; a < active.size(); ++a) {
+            const ProbRes &p = probs[active[a]];
+            int nb = (int)std::min<long long>((p.n + per - 1) / per, p.ntiles);
+            nb = std::max(nb, 1);
+            const int rows = (p.n + nb - 1) / nb;
+            for (int r = 0; r < nb; ++r)
+                C.push_back({(int)a, r, nb, r * rows, std::min(p.n, (r + 1) * rows), 0});
+        }
+        if ((long long)C.size() > cap) return HLANC_OK;
+        if ((int)C.size() > nctas_cap || !C_d) {
+            if (C_d) cudaFree(C_d);
+            nctas_cap = (int)C.size() + 64;
+            CK(cudaMalloc(&C_d, sizeof(CycTileH) * nctas_cap));
+        }
+        if (!bars_d || nslots_cap > bars_cap) {
+            if (bars_d) cudaFree(bars_d);
+            bars_cap = nslots_cap;
+            CK(cudaMalloc(&bars_d, sizeof(unsigned) * bars_cap));
+        }
+        CK(cudaMemcpyAsync(C_d, C.data(), sizeof(CycTileH) * C.size(), cudaMemcpyHostToDevice, stream));
+        nctas = (int)C.size();
+        return HLANC_OK;
+    }
+    int bars_cap = 0;
+
+    // The steps of one extension: one cooperative launch, or the per-phase
+    // launches of launch_step.
+    void enqueue_steps(int steps) {
+        if (nctas > 0) {
+            (void)launch_cycle(P_d, C_d, nctas, bars_d, (int)active.size(), steps, stream);
+            return;
+        }
+        for (int s = 0; s < steps; ++s)
+            launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, cgs_flags(), one(), one_tr, stream);
     }
 
     // Rebuild the descriptor/tile tables and the mailbox layout for `active`.
@@ -479,6 +551,7 @@ public:
         }
         nstiles = (int)ST.size();
         if (!ST.empty()) CK(cudaMemcpyAsync(S_d, ST.data(), sizeof(SpmvTile) * ST.size(), cudaMemcpyHostToDevice, stream));
+        if ((rc_cycle = plan_cycle())) return rc_cycle;
         ntiles = (int)T.size();
         one_tr = 0;
         if (active.size() == 1) {
@@ -542,8 +615,7 @@ public:
         const int na = (int)active.size();
         if (!device_restart) launch_scatter(P_d, na, off_d, flag_d, mbox_d, stream);
         if (basis_nev > 0) launch_basis(P_d, T_d, ntiles, max_ncv, basis_bucket(basis_nev), basis_tc, stream);
-        for (int s = 0; s < steps; ++s) launch_step(P_d, T_d, ntiles, S_d, nstiles, s, fp32_any, false, cgs_flags(), one(), one_tr,
-                                                    stream);
+        enqueue_steps(steps);
         if (device_restart) launch_restart(P_d, na, max_ncv, stream);
         launch_gather(P_d, na, off_d, mbox_d, stream);
     }
@@ -832,6 +904,14 @@ void fill_profile(const State &S, const ProbRes &p, double nnz, int fp32) {
     P.flops[KC_RITZ] = 2.0 * n * m * m;
     P.launches[KC_HOST] = g_prof->host_n;
     P.ms[KC_HOST] = g_prof->host_ms;
+    if (P.launches[KC_CYCLE] > 0) {     // the extensions ran as one launch each: their bytes are class 7's
+        for (int c : {KC_SPMV, KC_PROJ, KC_APPLY}) {
+            if (P.launches[c] > 0) continue;
+            P.bytes[KC_CYCLE] += P.bytes[c];
+            P.flops[KC_CYCLE] += P.flops[c];
+            P.bytes[c] = P.flops[c] = 0.0;
+        }
+    }
     g_have_prof = true;
 }
 
@@ -907,6 +987,7 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
     if (rc) return rc;
     E.basis_tc = o.basis_kernel != HLANC_BASIS_FP64;
     E.cgs_mode = o.cgs_kernel;
+    E.cycle_mode = o.cycle_kernel;
     const bool fp32 = csr && o.precision == HLANC_PREC_FP32_REFINE && csr->val32_d;
     int idx = 0;
     const hlanc_opts_t o1 = fp32 ? fp32_phase_opts(o) : o;
@@ -1030,6 +1111,8 @@ void hlanc_opts_default(hlanc_opts_t *o) {
     o->profile = 0;
     o->basis_kernel = HLANC_BASIS_AUTO;
     o->cgs_kernel = HLANC_CGS_AUTO;
+    o->wait_limit = 0;
+    o->cycle_kernel = HLANC_CYCLE_AUTO;
 }
 
 int hlanc_last_profile(hlanc_profile_t *out) {
@@ -1134,12 +1217,15 @@ int hlanc_csr_create(int dev, int nrows, int ncols, int nnz, const int *row_ptr,
     std::unique_ptr<hlanc_csr_s> h(new hlanc_csr_s());
     h->dev = dev; h->nrows = nrows; h->ncols = ncols; h->precision = precision; h->nnz = gnnz;
     double ninf = 0.0;
+    long long mrow = 0;
     for (int r = 0; r < nrows; ++r) {
         double s = 0.0;
         for (int i = grp[r]; i < grp[r + 1]; ++i) s += fabs(gva[i]);
         ninf = std::max(ninf, s);
+        mrow = std::max<long long>(mrow, grp[r + 1] - grp[r]);
     }
     h->norm_inf = ninf;
+    h->max_row = mrow;
     build_spmv_tiles(grp, nrows, h->stiles_h);
     DevGuard g(dev);
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
@@ -1485,6 +1571,7 @@ int hlanc_batch_create(int dev, int nprob, const hlanc_csr_t *ops, const int *ne
     if (rc) return rc;
     b->E.basis_tc = b->o.basis_kernel != HLANC_BASIS_FP64;
     b->E.cgs_mode = b->o.cgs_kernel;
+    b->E.cycle_mode = b->o.cycle_kernel;
     if (nprob > 1) b->E.min_tile_rows = BATCH_MIN_TILE_ROWS;
     const bool fp32 = b->o.precision == HLANC_PREC_FP32_REFINE;
     const hlanc_opts_t o1 = fp32 ? fp32_phase_opts(b->o) : b->o;
@@ -1865,9 +1952,7 @@ int srv_launch(Srv &s, Srv::Lane &L) {
     if (ritz) launch_ritz(E.P_d, E.T_d, E.ntiles, E.max_ncv, E.stream);
     if (basis_nev > 0)
         launch_basis(E.P_d, E.T_d, E.ntiles, E.max_ncv, Engine::basis_bucket(basis_nev), E.basis_tc, E.stream);
-    for (int k = 0; k < steps; ++k)
-        launch_step(E.P_d, E.T_d, E.ntiles, E.S_d, E.nstiles, k, E.fp32_any, false, E.cgs_flags(), E.one(),
-                    E.one_tr, E.stream);
+    E.enqueue_steps(steps);
     launch_gather(E.P_d, na, E.off_d, E.mbox_d, E.stream);
     if ((rc = E.pull_async())) return rc;
     CK(cudaEventRecord(L.ev1, E.stream));

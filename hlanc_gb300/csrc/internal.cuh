@@ -57,7 +57,7 @@ struct State {
 
 // Error codes a kernel leaves in State::err (the host returns them as
 // HLANC_ERR_DEVICE_TIMEOUT).
-enum : int { DEV_ERR_NONE = 0, DEV_ERR_MMA_WAIT = 1 };
+enum : int { DEV_ERR_NONE = 0, DEV_ERR_MMA_WAIT = 1, DEV_ERR_GRID_WAIT = 2 };
 constexpr int WAIT_LIMIT_DEFAULT = 1 << 20;   // far above any real wait
 
 // offsets (in doubles) of the per-problem small arrays, m = ncv
@@ -288,7 +288,8 @@ __device__ __forceinline__ const double *step_in(const Problem &P, int j) { retu
 __device__ __forceinline__ double *step_out(const Problem &P, int j) { return (j & 1) ? P.r0 : P.r1; }
 
 // ---- launch profiling (engine.cu): CUDA events around each launch ---------
-enum : int { KC_SPMV = 0, KC_PROJ = 1, KC_APPLY = 2, KC_BASIS = 3, KC_RITZ = 4, KC_AUX = 5, KC_HOST = 6 };
+enum : int { KC_SPMV = 0, KC_PROJ = 1, KC_APPLY = 2, KC_BASIS = 3, KC_RITZ = 4, KC_AUX = 5, KC_HOST = 6,
+             KC_CYCLE = 7 };
 void prof_begin(cudaStream_t s);
 void prof_end(int cls, cudaStream_t s);
 
@@ -328,6 +329,15 @@ void launch_scatter(const Problem *P_d, int nprob, const long long *off_d, const
 void launch_residuals(const int *row_ptr, const int *col, const double *val, int n, int k,
                       const double *values_d, const double *vectors_d, int ldv, double *out4k,
                       cudaStream_t s);
+
+// Whole Lanczos extensions in one cooperative launch (kernels_cycle.cu):
+// tiles_d holds one CycTile per CTA (problem slot, rank in its group, group
+// size, rows); bars_d one barrier counter per problem slot, zeroed here.
+int cycle_capacity();
+int cycle_rows_per_cta();
+struct CycTileH { int prob, rank, nb, row0, row1, pad; };
+cudaError_t launch_cycle(const Problem *P_d, const void *tiles_d, int nctas, unsigned *bars_d, int nprob, int steps,
+                         cudaStream_t s);
 
 // Kernels this library launched (all host threads), and launches per
 // kernel variant (HLANC_KL_*).

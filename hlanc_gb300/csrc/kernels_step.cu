@@ -81,9 +81,9 @@ __global__ void __launch_bounds__(TPB) k_norm_init(const Problem *__restrict__ p
 // solver on GB300 this beats staging the rows through shared memory (the
 // staged form waits on its copies before the gathers can start).
 constexpr int STAGE = 256;
-template <typename T, typename Emit>
+template <typename T, typename XL, typename Emit>
 __device__ __forceinline__ void spmv_short(const int *__restrict__ rp, const int *__restrict__ ci,
-                                           const T *__restrict__ val, const T *__restrict__ x, int row0,
+                                           const T *__restrict__ val, XL x, int row0,
                                            int row1, int *, T *, Emit emit) {
     for (int r = row0 + threadIdx.x; r < row1; r += TPB) {
         const int a = rp[r], b = rp[r + 1];
@@ -94,7 +94,7 @@ __device__ __forceinline__ void spmv_short(const int *__restrict__ rp, const int
             for (int q = 0; q < 8; ++q) {
                 const bool ok = i + q < b;
                 vv[q] = ok ? val[i + q] : T(0);
-                xv[q] = ok ? x[ci[i + q]] : T(0);
+                xv[q] = ok ? x(ci[i + q]) : T(0);
             }
 #pragma unroll
             for (int q = 0; q < 8; ++q)
@@ -107,9 +107,9 @@ __device__ __forceinline__ void spmv_short(const int *__restrict__ rp, const int
 // Short rows of uneven length (power-law graphs): LANES lanes per row, so a
 // warp waits on the longest of 32 / LANES rows instead of 32, and the lanes
 // of a row read its entries contiguously; a shuffle tree sums the row.
-template <typename T, int LANES, typename Emit>
+template <typename T, int LANES, typename XL, typename Emit>
 __device__ __forceinline__ void spmv_subwarp(const int *__restrict__ rp, const int *__restrict__ ci,
-                                             const T *__restrict__ val, const T *__restrict__ x, int row0,
+                                             const T *__restrict__ val, XL x, int row0,
                                              int row1, Emit emit) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int RPW = 32 / LANES;                 // rows per warp at a time
@@ -122,11 +122,11 @@ __device__ __forceinline__ void spmv_subwarp(const int *__restrict__ rp, const i
             int i = a + q;
             for (; i + LANES < b; i += 2 * LANES) {
                 const T v0 = val[i], v1 = val[i + LANES];
-                const T x0 = x[ci[i]], x1 = x[ci[i + LANES]];
+                const T x0 = x(ci[i]), x1 = x(ci[i + LANES]);
                 acc = fma(v0, x0, acc);
                 acc = fma(v1, x1, acc);
             }
-            if (i < b) acc = fma(val[i], x[ci[i]], acc);
+            if (i < b) acc = fma(val[i], x(ci[i]), acc);
         }
 #pragma unroll
         for (int o = LANES / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -135,14 +135,14 @@ __device__ __forceinline__ void spmv_subwarp(const int *__restrict__ rp, const i
 }
 
 // Wide row: whole CTA; the sum is valid in thread 0.
-template <typename T>
+template <typename T, typename XL>
 __device__ __forceinline__ T spmv_wide(const int *__restrict__ rp, const int *__restrict__ ci,
-                                       const T *__restrict__ val, const T *__restrict__ x, int r, T *red) {
+                                       const T *__restrict__ val, XL x, int r, T *red) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int a = rp[r], b = rp[r + 1];
     T acc = T(0);
 #pragma unroll 4
-    for (int i = a + threadIdx.x; i < b; i += TPB) acc = fma(val[i], x[ci[i]], acc);
+    for (int i = a + threadIdx.x; i < b; i += TPB) acc = fma(val[i], x(ci[i]), acc);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     __syncthreads();
@@ -154,9 +154,10 @@ __device__ __forceinline__ T spmv_wide(const int *__restrict__ rp, const int *__
     return sum;
 }
 
-template <typename T, typename Emit>
+// x: a functor giving x[c] (a plain load, or a conversion on the fly).
+template <typename T, typename XL, typename Emit>
 __device__ __forceinline__ void spmv_unit(const SpmvTile &t, const int *__restrict__ rp, const int *__restrict__ ci,
-                                          const T *__restrict__ val, const T *__restrict__ x, int *s_col,
+                                          const T *__restrict__ val, XL x, int *s_col,
                                           T *s_val, T *red, Emit emit) {
     if (t.kind == 0) {
         spmv_short<T>(rp, ci, val, x, t.row0, t.row1, s_col, s_val, emit);
@@ -172,20 +173,32 @@ __device__ __forceinline__ void spmv_unit(const SpmvTile &t, const int *__restri
     }
 }
 
+template <typename T>
+struct XLoad {
+    const T *__restrict__ p;
+    __device__ __forceinline__ T operator()(int c) const { return p[c]; }
+};
+// FP32 copy of the Lanczos vector v = r / rnorm, rounded as it is gathered
+struct XLoadF32 {
+    const double *__restrict__ r;
+    double t1;
+    __device__ __forceinline__ float operator()(int c) const { return (float)(r[c] * t1); }
+};
+
 // ---- SpMV of the step --------------------------------------------------------
 // One CTA per SpMV unit (the hardware scheduler balances skewed units).
 // v_j -> V[:, j] for the unit's rows, w = A v_j (FP64: A r, one scaling per row;
-// in the FP32 form k_prep wrote V[:, j] and its FP32 copy beforehand).
+// FP32: x = (float)(r / rnorm) formed as it is gathered).
 // Six resident CTAs per SM (40 registers) keep enough gathers in flight: on
 // GB300 this measured 18% faster than the unbounded 72-register build on the
 // 4.1M-row Laplacian (70% of HBM standalone) and 14% faster on the power-law
 // graph; streaming (evict-first) loads of the entries were slower, because
-// neighbouring rows share their cache sectors.  The FP32 step kernel runs at
-// 5 CTAs per SM: at 6 it spilled, and 5 measured 0.5% faster on the
-// mixed-precision power-law solve.
+// neighbouring rows share their cache sectors.  The FP32 step kernel, which
+// also rounds the vector to FP32 as it gathers it and writes V[:, j], runs
+// at 4 CTAs per SM (at 5 it spills).
 constexpr int SPMV_CTAS_PER_SM = 6;
 template <bool F32>
-__global__ void __launch_bounds__(TPB, F32 ? 5 : SPMV_CTAS_PER_SM) k_spmv_step(const Problem *__restrict__ probs,
+__global__ void __launch_bounds__(TPB, F32 ? 4 : SPMV_CTAS_PER_SM) k_spmv_step(const Problem *__restrict__ probs,
                                                    const SpmvTile *__restrict__ tiles, int ntiles, int s) {
     using T = typename std::conditional<F32, float, double>::type;
     __shared__ int s_col[(TPB / 32) * STAGE];
@@ -205,12 +218,20 @@ __global__ void __launch_bounds__(TPB, F32 ? 5 : SPMV_CTAS_PER_SM) k_spmv_step(c
     double *__restrict__ vj = P.V + (size_t)j * P.ld;
     float *__restrict__ vj32 = P.V32 + (size_t)j * P.ld;
     if constexpr (F32) {
-        spmv_unit<float>(t, P.row_ptr, P.col, P.val32, P.x32, s_col, s_val, red,
-                         [=](int rr, float acc) { w[rr] = (double)acc; });
+        // FP32 values, the vector rounded to FP32 as it is gathered, FP32
+        // accumulation; V[:, j] (FP64) is written where each row is emitted
+        spmv_unit<float>(t, P.row_ptr, P.col, P.val32, XLoadF32{rin, t1}, s_col, s_val, red,
+                         [=](int rr, float acc) {
+                             const double x = rin[rr];
+                             const double v = scale ? x * t1 : x;
+                             w[rr] = (double)acc;
+                             vj[rr] = v;
+                             vj32[rr] = (float)v;
+                         });
     } else {
         // each row is emitted once: V[:, j] is written there too, instead of
         // in a separate pass over the unit's rows before the gathers start
-        spmv_unit<double>(t, P.row_ptr, P.col, P.val, rin, s_col, s_val, red, [=](int rr, double acc) {
+        spmv_unit<double>(t, P.row_ptr, P.col, P.val, XLoad<double>{rin}, s_col, s_val, red, [=](int rr, double acc) {
             const double x = rin[rr];
             const double v = scale ? x * t1 : x;
             w[rr] = scale ? acc * t1 : acc;
@@ -672,7 +693,7 @@ __global__ void __launch_bounds__(TPB, SPMV_CTAS_PER_SM) k_spmv_plain(const int 
     __shared__ T s_val[(TPB / 32) * STAGE];
     __shared__ T red[TPB / 32];
     for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
-        spmv_unit<T>(tiles[ti], rp, ci, val, x, s_col, s_val, red, [=](int rr, T acc) { y[rr] = acc; });
+        spmv_unit<T>(tiles[ti], rp, ci, val, XLoad<T>{x}, s_col, s_val, red, [=](int rr, T acc) { y[rr] = acc; });
 }
 
 // ---- residuals of k Ritz pairs (demo/verify_eigs.cu:52-98) ------------------
@@ -770,12 +791,9 @@ void launch_step(const Problem *P_d, const Tile *tiles_d, int ntiles, const Spmv
     if (!external_w) {
         if (fp32_any) {
             prof_begin(s);
-            (void)launch_pdl(k_prep, dim3(ntiles), dim3(TPB), s, P_d, tiles_d, step, 0, (double *)nullptr);
-            prof_end(KC_SPMV, s);
-            prof_begin(s);
             (void)launch_pdl(k_spmv_step<true>, dim3(spmv_grid(nstiles)), dim3(TPB), s, P_d, stiles_d, nstiles, step);
             prof_end(KC_SPMV, s);
-            launch_counter() += 2;
+            launch_counter() += 1;
         }
         prof_begin(s);
         (void)launch_pdl(k_spmv_step<false>, dim3(spmv_grid(nstiles)), dim3(TPB), s, P_d, stiles_d, nstiles, step);

@@ -50,7 +50,9 @@ constexpr int BM = 128;       // rows per block = MMA M
 constexpr int NDIG = 7;       // digit planes / levels
 constexpr int KMAX = 64;      // largest padded ncv
 constexpr int NMAX = 64;      // largest padded nev + 1
-constexpr int THREADS = 256;
+constexpr int THREADS = 512;
+constexpr int NQ = THREADS / BM;   // threads per row of a block (each loads and splits 1/NQ of its columns)
+constexpr int GMAX = (KMAX / 8 + NQ - 1) / NQ;   // 8-column groups per thread
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -274,7 +276,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
     unsigned char *sB = smem + (size_t)NDIG * BM * KMAX * 2;    // 7 x NPAD x kpad bf16
     __shared__ uint64_t s_mbar;
     __shared__ uint32_t s_taddr;
-    __shared__ int s_rowexp[2][BM];
+    __shared__ int s_rowexp[NQ][BM];
     __shared__ int s_colexp[NPAD];
     __shared__ double s_red[32], s_mine[1], s_tot[1];
     __shared__ int s_fail;
@@ -335,32 +337,44 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
     uint32_t phase = 0;
 
     // loader mapping: row r of the block, groups g0.. of 8 columns
-    const int lr = tid & (BM - 1), half = tid >> 7;
-    const int gper = (kg + 1) >> 1, g0 = half * gper, g1 = min(kg, g0 + gper);
+    const int lr = tid & (BM - 1), part = tid / BM;
+    const int gper = (kg + NQ - 1) / NQ, g0 = part * gper, g1 = min(kg, g0 + gper);
 
-    for (int R0 = t.row0; R0 < t.row1; R0 += BM) {
-        prefetch_rows_l2(P.V, ld, m, R0 + BM, min(BM, t.row1 - (R0 + BM)));
-        // 1. load this thread's part of row R0 + lr and its largest exponent
+    // this thread's part of row R0 + lr (zeros past the tile / past ncv)
+    auto load_rows = [&](int R0, double (&x)[GMAX][8]) {
         const int row = R0 + lr;
         const bool rok = row < t.row1;
-        double x[4][8];
-        int emax = 0;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < GMAX; ++q) {
             const int g = g0 + q;
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
                 const int k = 8 * g + e;
                 x[q][e] = (rok && g < g1 && k < m) ? P.V[row + (size_t)k * ld] : 0.0;
-                emax = max(emax, exp_field(x[q][e]));
             }
         }
-        s_rowexp[half][lr] = emax;
+    };
+    double x[GMAX][8];
+    prefetch_rows_l2(P.V, ld, m, t.row0 + BM, min(BM, t.row1 - (t.row0 + BM)));
+    load_rows(t.row0, x);
+
+    for (int R0 = t.row0; R0 < t.row1; R0 += BM) {
+        prefetch_rows_l2(P.V, ld, m, R0 + 2 * BM, min(BM, t.row1 - (R0 + 2 * BM)));
+        // 1. the largest exponent of each row (x holds this block, loaded
+        //    while the previous block's products ran)
+        int emax = 0;
+#pragma unroll
+        for (int q = 0; q < GMAX; ++q)
+#pragma unroll
+            for (int e = 0; e < 8; ++e) emax = max(emax, exp_field(x[q][e]));
+        s_rowexp[part][lr] = emax;
         __syncthreads();
-        const int ex = max(s_rowexp[0][lr], s_rowexp[1][lr]);
+        int ex = s_rowexp[0][lr];
+#pragma unroll
+        for (int q = 1; q < NQ; ++q) ex = max(ex, s_rowexp[q][lr]);
         // 2. digit planes of the block
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < GMAX; ++q) {
             const int g = g0 + q;
             if (g >= g1) break;
             uint4 pl[NDIG];
@@ -392,6 +406,9 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
             }
             mma_commit(&s_mbar);
         }
+        // 3b. the next block's rows load while the products run (x is free
+        //     after the split; the recombine below writes other rows)
+        if (R0 + BM < t.row1) load_rows(R0 + BM, x);
         // 4. wait for the products (bounded).  A wait that gives up marks the
         //    CTA failed, then waits (again bounded) for the MMAs it already
         //    issued, so tensor memory is not released under them.
@@ -409,16 +426,18 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
         fence_after();
         __syncthreads();
         if (s_fail) break;
-        // 5. recombine: warp w reads TMEM lanes 32 (w % 4) .. +31; the two warps of a
-        //    lane quarter take alternate groups of 4 outputs
+        // 5. recombine: warp w reads TMEM lanes 32 (w % 4) .. +31; the four warps of a
+        //    lane quarter take every fourth group of 4 outputs
         {
             const int q4 = warp & 3, ch = warp >> 2;
             const int r = 32 * q4 + lane;
             const int orow = R0 + r;
             const bool ok = orow < t.row1;
-            const int exr = max(s_rowexp[0][r], s_rowexp[1][r]);
+            int exr = s_rowexp[0][r];
+#pragma unroll
+            for (int q = 1; q < NQ; ++q) exr = max(exr, s_rowexp[q][r]);
             const uint32_t lane_base = taddr + ((uint32_t)(32 * q4) << 16);
-            for (int c0 = ch * 4; c0 < nout; c0 += 8) {
+            for (int c0 = ch * 4; c0 < nout; c0 += 4 * (THREADS / 128)) {
                 float d[NDIG][4];
                 tmem_ld_levels4(lane_base + (uint32_t)c0, (uint32_t)NPAD, d);
 #pragma unroll

@@ -55,6 +55,14 @@ extern "C" {
 #define HLANC_CGS_FP64            1  /* every column of both passes as FP64 FMAs */
 #define HLANC_CGS_HYBRID          2  /* hybrid projection at every size; update as AUTO */
 
+/* How a restart cycle's Lanczos steps are launched (hlanc_opts_t.cycle_kernel).
+ * A problem too small to fill the GPU is latency-bound when every step is
+ * seven launches; one cooperative launch can run the whole extension, its
+ * CTAs meeting at bounded group barriers between the phases of a step. */
+#define HLANC_CYCLE_AUTO          0  /* one launch per extension when every problem of the launch has
+                                        rows of <= 96 entries and they have <= 49,152 rows in total */
+#define HLANC_CYCLE_OFF           1  /* always the per-phase launches */
+
 /* Largest ncv the device restart kernels accept, and largest nev. */
 #define HLANC_MAX_NCV           128
 #define HLANC_MAX_NEV            63
@@ -124,7 +132,8 @@ typedef struct {
     int wait_limit;           /* polls of each bounded device wait before it gives up and the
                                  solve returns HLANC_ERR_DEVICE_TIMEOUT: 0 = default (2^20),
                                  < 0 = give up at once (tests of the failure path) */
-    int reserved[2];
+    int cycle_kernel;         /* HLANC_CYCLE_*; default HLANC_CYCLE_AUTO */
+    int reserved[1];
 } hlanc_opts_t;
 
 /* Fill defaults (tol 0, max_restarts 200, FP64, seed 0, graphs on, host restart). */
@@ -266,15 +275,18 @@ long long hlanc_kernel_launches(void);
 #define HLANC_KL_APPLY_FP64       4  /* CGS update, all FP64 */
 #define HLANC_KL_BASIS_TC         5  /* restart basis update on the tensor cores */
 #define HLANC_KL_BASIS_FP64       6  /* restart basis update on FP64 CUDA cores */
-#define HLANC_KL_KINDS            7
+#define HLANC_KL_CYCLE            7  /* a whole Lanczos extension in one cooperative launch */
+#define HLANC_KL_KINDS            8
 long long hlanc_kernel_launches_of(int kind);
 
 /* Per-kernel-class timing of the last solve run with opts.profile = 1 on the
  * calling thread.  Classes: 0 SpMV, 1 CGS projection, 2 CGS update,
  * 3 basis update (V*Q), 4 Ritz vectors, 5 auxiliary kernels, 6 host restart
- * (CPU time).  bytes / flops are the algorithmic DRAM bytes and FP64 flops
- * of the launches that did work. */
-#define HLANC_PROF_CLASSES 7
+ * (CPU time), 7 whole extensions in one launch (HLANC_CYCLE_AUTO on small
+ * problems; their SpMV and CGS bytes are counted here, not in 0-2).
+ * bytes / flops are the algorithmic DRAM bytes and FP64 flops of the
+ * launches that did work. */
+#define HLANC_PROF_CLASSES 8
 typedef struct {
     long long launches[HLANC_PROF_CLASSES];
     double ms[HLANC_PROF_CLASSES];

@@ -46,13 +46,22 @@ def test_device_restart_path_agrees(H):
 def test_profile_classes(H):
     m = G.laplacian_3d(20, shift_seed=1)
     op = H.dcsrmv_operator_gpu(m)
-    rc, vals, _, st = H.solve(op, 10, 30, tol=1e-10, profile=True)
+    # per-phase launches
+    rc, vals, _, st = H.solve(op, 10, 30, tol=1e-10, profile=True, cycle=H.HLANC_CYCLE_OFF)
     assert rc == 0
     p = H.last_profile()
     assert p["spmv"]["launches"] >= st["spmv_calls"]
     assert p["cgs_proj"]["launches"] > 0 and p["cgs_proj"]["ms"] > 0
     assert p["cgs_apply"]["bytes"] > 0 and p["basis"]["launches"] > 0
     assert p["host_restart"]["launches"] == st["restarts"]
+    assert p["cycle"]["launches"] == 0
+    # the default on a problem this small: one launch per extension
+    rc2, vals2, _, st2 = H.solve(op, 10, 30, tol=1e-10, profile=True)
+    assert rc2 == 0
+    p = H.last_profile()
+    assert p["cycle"]["launches"] == st2["restarts"] and p["cycle"]["bytes"] > 0
+    assert p["spmv"]["launches"] == 0 and p["cgs_proj"]["launches"] == 0
+    assert np.abs(vals2[:10] - vals[:10]).max() <= 1e-10 * np.abs(vals[:10]).max()
 
 
 def test_residual_verifier(H, torch):
