@@ -68,6 +68,9 @@ WORKLOADS = {
                        gen=lambda: G.chung_lu_normalized(1 << 22, seed=2), nev=16, ncv=48, tol=1e-10, mixed=True),
     "chunglu_22_fp64": dict(desc="normalised adjacency of a Chung-Lu graph, n = 2^22 (seed 2); plain FP64",
                             gen=lambda: G.chung_lu_normalized(1 << 22, seed=2), nev=16, ncv=48, tol=1e-10),
+    "chunglu_20_fp64": dict(desc="normalised adjacency of a Chung-Lu graph, n = 2^20 (seed 2); plain FP64 "
+                                 "(the power-law workload at a size for kernel profiles)",
+                            gen=lambda: G.chung_lu_normalized(1 << 20, seed=2), nev=16, ncv=48, tol=1e-10),
 }
 
 # Reference fixture of each workload (tests/golden/<name>.npz, written from
@@ -243,9 +246,34 @@ def cpu_sample(m, wl, threads, full_spmv, full_src):
                 seconds_per_step=per_step, sample_seconds=dt, extrapolated_seconds=est)
 
 
+def calibrated_cpu_spmv(workload):
+    """Operator applications of the oracle's own full CPU solve of the
+    workload at its tolerance, from the committed calibration record
+    (profiles/*.txt line 'cpu_full_solve_spmv <workload> <count>', written
+    from a --calibrate-cpu run on the GPU machine's host)."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if fn.endswith(".txt"):
+            with open(os.path.join(d, fn)) as f:
+                for line in f:
+                    p = line.split()
+                    if len(p) == 3 and p[0] == "cpu_full_solve_spmv" and p[1] == workload:
+                        return int(p[2])
+    return None
+
+
 def full_spmv_count(args, wl, gpu_count=None):
+    """Operator applications of a full CPU solve of the workload: the
+    oracle's calibration run at the workload's tolerance, else the
+    reference's own golden solve when the workload uses the reference's
+    tolerance (dlamch('E')), else this library's count (stated)."""
+    c = calibrated_cpu_spmv(args.workload)
+    if c:
+        return c, "the oracle's own full CPU solve at this tolerance (calibration record, profiles/)"
     g = golden_of(args.workload)
-    if g is not None:
+    if g is not None and not wl["tol"]:
         return int(g["spmv_calls"]), "the reference's own full CPU solve (tests/golden)"
     if args.full_spmv:
         return args.full_spmv, "--full-spmv"

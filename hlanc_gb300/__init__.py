@@ -62,7 +62,7 @@ class Stats(C.Structure):
                 ("nconv", C.c_int), ("refine_restarts", C.c_int), ("status", C.c_int),
                 ("rnorm", C.c_double), ("seconds", C.c_double), ("bytes_spmv", C.c_double),
                 ("bytes_cgs", C.c_double), ("bytes_restart", C.c_double), ("cgs_update_fp32_share", C.c_double),
-                ("reserved", C.c_double * 3)]
+                ("refine_residual", C.c_double), ("reserved", C.c_double * 2)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -121,6 +121,7 @@ def _declare(L):
         "hlanc_csr_apply": (_i, [_p, _p, _p]),
         "hlanc_csr_spmv_async": (_i, [_p, _p, _p, _p]),
         "hlanc_csr_spmv_f32_async": (_i, [_p, _p, _p, _p]),
+        "hlanc_csr_tuning": (_i, [_p, _ip, _ip, _ip, _dp, _dp]),
         "hlanc_solve": (_i, [_i, _i, _i, _i, _p, _p, _i, _p, HOST_OP, _p, C.POINTER(Opts),
                              C.POINTER(Stats)]),
         "hlanc_solve_device": (_i, [_i, _i, _i, _i, _p, _p, _i, _p, C.POINTER(Opts), C.POINTER(Stats)]),
@@ -293,6 +294,15 @@ class dcsrmv_operator_gpu:
         if ny and (y.dtype != np.float64 or not y.flags.c_contiguous or not y.flags.writeable):
             raise TypeError("y must be a writable contiguous float64 array")
         _check(lib().hlanc_csr_apply(self._h, px, py), "operator()")
+
+    def tuning(self) -> dict:
+        """SpMV work units chosen for this matrix (hlanc_csr_tuning)."""
+        r, l4, l8 = _i(), _i(), _i()
+        ud, uc = C.c_double(), C.c_double()
+        _check(lib().hlanc_csr_tuning(self._h, C.byref(r), C.byref(l4), C.byref(l8), C.byref(ud), C.byref(uc)),
+               "tuning")
+        return {"rows_per_unit": r.value, "lanes4_mean": l4.value, "lanes8_mean": l8.value,
+                "us_default": ud.value, "us_chosen": uc.value}
 
     def spmv_async(self, x_ptr: int, y_ptr: int, stream: int = 0) -> None:
         _check(lib().hlanc_csr_spmv_async(self._h, x_ptr, y_ptr, stream or None), "spmv_async")

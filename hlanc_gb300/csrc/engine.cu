@@ -59,15 +59,22 @@ struct hlanc_csr_s {
     cudaStream_t stream = nullptr;
     double norm_inf = 0.0;                      // max_r sum |a_rc|
     long long max_row = 0;                      // longest row (entries), general CSR
+    int tune[4] = {SPMV_ROWS, SPMV_NNZ, SUBWARP4_MEAN, SUBWARP8_MEAN};   // SpMV unit shape in use
+    double tune_us = 0.0, tune_us_default = 0.0;   // measured SpMV time of it / of the default (0: not tuned)
     std::vector<SpmvTile> stiles_h;             // entry-balanced SpMV work units (prob = 0)
     SpmvTile *stiles_d = nullptr;
     std::mutex mu;
 };
 
 // Split rows into SpMV work units (see SpmvTile): runs of short rows (at most
-// SPMV_ROWS rows / SPMV_NNZ entries; thread, 4 or 8 lanes per row by the
-// run's mean length), runs of up to TPB/16 medium rows, and single wide rows.
-static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &out) {
+// prm.rows rows / prm.nnz entries; thread, 4 or 8 lanes per row by the run's
+// mean length against prm.sub4 / prm.sub8), runs of up to TPB/16 medium rows,
+// and single wide rows.
+struct SpmvParams { int rows, nnz, sub4, sub8; };
+constexpr SpmvParams SPMV_DEFAULT = {SPMV_ROWS, SPMV_NNZ, SUBWARP4_MEAN, SUBWARP8_MEAN};
+
+static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &out,
+                             const SpmvParams &prm = SPMV_DEFAULT) {
     out.clear();
     auto len = [&](int r) { return (long long)rp[r + 1] - rp[r]; };
     int r = 0;
@@ -83,14 +90,78 @@ static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &ou
         } else {
             const int r0 = r;
             long long nnz = 0;
-            while (r < nrows && r - r0 < SPMV_ROWS && len(r) <= LONG_ROW && nnz + len(r) <= SPMV_NNZ) {
+            while (r < nrows && r - r0 < prm.rows && len(r) <= LONG_ROW && nnz + len(r) <= prm.nnz) {
                 nnz += len(r);
                 ++r;
             }
             const long long mean = nnz / (r - r0);
-            out.push_back({0, r0, r, mean > SUBWARP8_MEAN ? 4 : (mean > SUBWARP4_MEAN ? 3 : 0)});
+            out.push_back({0, r0, r, mean > prm.sub8 ? 4 : (mean > prm.sub4 ? 3 : 0)});
         }
     }
+}
+
+// SpMV units tuned per matrix.  The row-length histogram decides whether
+// there is anything to choose: when no row has more than SUBWARP4_MEAN
+// entries, every short unit runs thread per row whatever the thresholds and
+// the default units stand (the Laplacians).  Otherwise a few unit shapes --
+// rows per unit and the mean row lengths at which a unit takes 4 / 8 lanes
+// per row -- are built and each SpMV is timed on the device (one warm-up,
+// best of three, CUDA events), and the fastest is kept.  Problems of fewer
+// than 2^16 rows keep the default: their SpMV is launch-latency bound.
+static int autotune_spmv(hlanc_csr_s *h, const int *grp) {
+    if (h->nrows < (1 << 16) || h->max_row <= SUBWARP4_MEAN) return HLANC_OK;
+    const SpmvParams cand[] = {SPMV_DEFAULT, {256, 4096, SUBWARP4_MEAN, SUBWARP8_MEAN}, {1024, 16384, 6, 16},
+                               {1024, 16384, 24, 64}, {1024, 16384, 1 << 30, 1 << 30}};
+    const int nc = (int)(sizeof cand / sizeof cand[0]);
+    cudaStream_t s = h->stream;
+    CK(cudaMemsetAsync(h->xs_d, 0, sizeof(double) * (size_t)std::max(h->ncols, 1), s));
+    struct Res {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        SpmvTile *t = nullptr;
+        ~Res() { if (e0) cudaEventDestroy(e0); if (e1) cudaEventDestroy(e1); if (t) cudaFree(t); }
+    } r;
+    CK(cudaEventCreate(&r.e0));
+    CK(cudaEventCreate(&r.e1));
+    std::vector<std::vector<SpmvTile>> tiles(nc);
+    size_t cap = 0;
+    for (int c = 0; c < nc; ++c) {
+        build_spmv_tiles(grp, h->nrows, tiles[c], cand[c]);
+        cap = std::max(cap, tiles[c].size());
+    }
+    CK(cudaMalloc(&r.t, sizeof(SpmvTile) * std::max<size_t>(cap, 1)));
+    int best = 0;
+    std::vector<double> us(nc, 0.0);
+    for (int c = 0; c < nc; ++c) {
+        const int nt = (int)tiles[c].size();
+        if (!nt) continue;
+        CK(cudaMemcpyAsync(r.t, tiles[c].data(), sizeof(SpmvTile) * nt, cudaMemcpyHostToDevice, s));
+        launch_spmv(h->rp_d, h->ci_d, h->val_d, r.t, nt, h->xs_d, h->ys_d, s);
+        float bestms = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            CK(cudaEventRecord(r.e0, s));
+            launch_spmv(h->rp_d, h->ci_d, h->val_d, r.t, nt, h->xs_d, h->ys_d, s);
+            CK(cudaEventRecord(r.e1, s));
+            CK(cudaEventSynchronize(r.e1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, r.e0, r.e1));
+            bestms = std::min(bestms, ms);
+        }
+        us[c] = bestms * 1e3;
+        if (us[c] < us[best]) best = c;
+    }
+    h->tune_us_default = us[0];
+    h->tune_us = us[best];
+    h->tune[0] = cand[best].rows; h->tune[1] = cand[best].nnz; h->tune[2] = cand[best].sub4; h->tune[3] = cand[best].sub8;
+    if (best != 0) {
+        h->stiles_h.swap(tiles[best]);
+        CK(cudaFree(h->stiles_d));
+        h->stiles_d = nullptr;
+        CK(cudaMalloc(&h->stiles_d, sizeof(SpmvTile) * std::max<size_t>(h->stiles_h.size(), 1)));
+        CK(cudaMemcpyAsync(h->stiles_d, h->stiles_h.data(), sizeof(SpmvTile) * h->stiles_h.size(),
+                           cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    return HLANC_OK;
 }
 
 struct hlanc_matrix_s {
@@ -189,7 +260,6 @@ struct ProbRes {
     float *V32 = nullptr;      // FP32 shadow of V (ld x ncv)
     State *st = nullptr;
     unsigned *counter = nullptr;
-    float *x32 = nullptr;
     double *vout = nullptr;
     int ldo = 0;
     bool own_vout = false;
@@ -210,7 +280,6 @@ struct ProbRes {
         const size_t pst = (size_t)((ncv + 2 + 1) & ~1);
         size_t d = ld * ncv + 2 * ld + (nt + ng) * pst + SM_SIZE(ncv);
         size_t b = d * sizeof(double) + 1024 + 4 * ng;
-        if (fp32) b += ld * sizeof(float);
         b += ld * ncv * sizeof(float);    // FP32 shadow of the basis
         b += ld * ncv * sizeof(double);   // Ritz output
         return b;
@@ -250,11 +319,6 @@ struct ProbRes {
         st = (State *)sp;
         counter = (unsigned *)((char *)sp + 512);
         bytes += sb;
-        if (fp32) {
-            CK(dmalloc((void **)&x32, (size_t)ld * sizeof(float), s));
-            CK(cudaMemsetAsync(x32, 0, (size_t)ld * sizeof(float), s));
-            bytes += (size_t)ld * sizeof(float);
-        }
         CK(dmalloc((void **)&V32, (size_t)ld * ncv * sizeof(float), s));
         CK(cudaMemsetAsync(V32, 0, (size_t)ld * ncv * sizeof(float), s));
         bytes += (size_t)ld * ncv * sizeof(float);
@@ -275,10 +339,9 @@ struct ProbRes {
     void release() {
         dfree(block);
         dfree(st);
-        dfree(x32);
         dfree(V32);
         if (own_vout) dfree(vout);
-        block = nullptr; st = nullptr; x32 = nullptr; V32 = nullptr; vout = nullptr; own_vout = false;
+        block = nullptr; st = nullptr; V32 = nullptr; vout = nullptr; own_vout = false;
         live = false;
     }
 };
@@ -492,7 +555,6 @@ public:
                 q.row_ptr = p.csr->rp_d; q.col = p.csr->ci_d; q.val = p.csr->val_d;
                 q.val32 = p.fp32 ? p.csr->val32_d : nullptr;
             }
-            q.x32 = p.x32;
             q.n = p.n; q.ld = p.ld; q.ncv = p.ncv; q.nev0 = p.nev0;
             q.tile0 = (int)T.size(); q.ntiles = p.ntiles;
             q.fp32 = p.fp32; q.pstride = p.pstride;
@@ -878,6 +940,7 @@ void fill_stats(hlanc_stats_t *stats, const State &S, const ProbRes &p, double n
     stats->bytes_cgs = 16.0 * n * (double)S.sumc - 4.0 * n * (double)S.sumt + 24.0 * n * (double)S.passes;
     stats->bytes_restart = (8.0 * n * p.ncv + 16.0 * n) * S.napply + 8.0 * n * (double)S.sumnev;
     stats->cgs_update_fp32_share = S.sumc > 0 ? (double)S.sumt / (double)S.sumc : 0.0;
+    stats->refine_residual = -1.0;
 }
 
 void fill_profile(const State &S, const ProbRes &p, double nnz, int fp32) {
@@ -958,8 +1021,8 @@ hlanc_opts_t fp32_phase_opts(const hlanc_opts_t &o) {
 }
 
 // Start vector of the FP64 phase, written into r0: the sum of the FP32
-// phase's Ritz vectors when it converged (they are in vout), else that
-// phase's current first Lanczos vector V[:, 0] -- the start vector its
+// phase's (refined) Ritz vectors when it converged (they are in vout), else
+// that phase's current first Lanczos vector V[:, 0] -- the start vector its
 // restarts have filtered so far.
 void fp64_phase_start(const ProbRes &p, cudaStream_t s) {
     if (p.hs.status == ST_CONVERGED && p.hs.fin == 2)
@@ -967,6 +1030,63 @@ void fp64_phase_start(const ProbRes &p, cudaStream_t s) {
     else
         k_sum_columns<<<304, 256, 0, s>>>(p.V, p.ld, p.n, 1, p.r0);
     launch_counter() += 1;
+}
+
+// FP64 Rayleigh-Ritz of the FP32 phase's k converged pairs (vout[:, 0:k)):
+// W = A Y with the FP64 operator, G = Y^T W, G = Z Theta Z^T (host Jacobi),
+// Y' = Y Z, and the FP64 residuals of (theta_i, y'_i) (the reference's Ritz
+// post-processing on its converged basis, HLanc.hpp:1765-1843, with true
+// residuals for its Ritz estimates, H:1693-1695).  The refined pairs replace
+// vout[:, 0:k) and the values in either case; *accepted when every residual
+// is <= tol ||A||_inf.  *resid_max is the largest residual / ||A||_inf.
+int refine_rr(Engine &E, ProbRes &p, double tol, bool *accepted, double *resid_max, long long *spmv_add) {
+    *accepted = false;
+    *resid_max = -1.0;
+    *spmv_add = 0;
+    const int k = p.hs.nconv, n = p.n, ldo = p.ldo;
+    hlanc_csr_s *c = p.csr;
+    if (!c || k < 1 || k > 64 || !p.vout) return HLANC_OK;
+    cudaStream_t s = E.stream;
+    const int nb = gram_blocks(n);
+    struct Tmp {
+        double *W = nullptr, *part = nullptr, *small = nullptr;
+        ~Tmp() { if (W) cudaFree(W); if (part) cudaFree(part); if (small) cudaFree(small); }
+    } t;
+    CK(cudaMalloc(&t.W, sizeof(double) * (size_t)ldo * k));
+    CK(cudaMalloc(&t.part, sizeof(double) * (size_t)nb * k * k));
+    CK(cudaMalloc(&t.small, sizeof(double) * (2 * (size_t)k * k + 5 * (size_t)k)));
+    double *G = t.small, *Zd = G + k * k, *th = Zd + k * k, *out4 = th + k;
+    const int nst = (int)c->stiles_h.size();
+    for (int i = 0; i < k; ++i)
+        launch_spmv(c->rp_d, c->ci_d, c->val_d, c->stiles_d, nst, p.vout + (size_t)i * ldo, t.W + (size_t)i * ldo, s);
+    launch_gram(p.vout, t.W, n, ldo, k, t.part, G, s);
+    std::vector<double> g((size_t)k * k), z((size_t)k * k), w(k), r4(4 * (size_t)k);
+    CK(cudaMemcpyAsync(g.data(), G, sizeof(double) * k * k, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int j = 0; j < k; ++j)
+        for (int i = 0; i < j; ++i) {
+            const double a = 0.5 * (g[i + (size_t)j * k] + g[j + (size_t)i * k]);
+            g[i + (size_t)j * k] = g[j + (size_t)i * k] = a;
+        }
+    if (host::sym_eig_jacobi(k, g.data(), w.data(), z.data())) return HLANC_OK;
+    CK(cudaMemcpyAsync(Zd, z.data(), sizeof(double) * k * k, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(th, w.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    launch_rotate(p.vout, n, ldo, k, Zd, t.W, s);
+    launch_residuals(c->rp_d, c->ci_d, c->val_d, n, k, th, t.W, ldo, out4, s);
+    CK(cudaMemcpyAsync(r4.data(), out4, sizeof(double) * 4 * k, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpy2DAsync(p.vout, sizeof(double) * ldo, t.W, sizeof(double) * ldo, sizeof(double) * n, k,
+                         cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(p.small + SM_VALS(p.ncv), th, sizeof(double) * k, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaGetLastError());
+    *spmv_add = 2LL * k;
+    double mx = 0.0;
+    for (int i = 0; i < k; ++i) mx = std::max(mx, sqrt(r4[4 * (size_t)i]));
+    const double na = c->norm_inf > 0 ? c->norm_inf : 1.0;
+    *resid_max = mx / na;
+    for (int i = 0; i < k; ++i) p.values[i] = w[i];
+    *accepted = tol > 0.0 && mx <= tol * na;
+    return HLANC_OK;
 }
 
 // Full solve of one problem.  values/vectors are host (device_out = false)
@@ -1002,9 +1122,24 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
     State S1 = p.hs;
     int refine_restarts = 0;
     State S = S1;
+    bool accepted = false;             // the refined FP32-phase pairs are the result
+    double rr_resid = -1.0;
     if (fp32) {
-        // FP64 phase warm-started from the FP32 phase
-        if (S1.status == ST_CONVERGED && (rc = E.finalize(idx))) return rc;
+        // FP64 Rayleigh-Ritz of the FP32 phase's pairs; FP64 restart cycles
+        // from the refined vectors where a residual misses the tolerance
+        if (S1.status == ST_CONVERGED) {
+            if ((rc = E.finalize(idx))) return rc;
+            if (p.hs.status == ST_CONVERGED && p.hs.fin == 2) {
+                long long rr_spmv = 0;
+                if ((rc = refine_rr(E, p, o.tol, &accepted, &rr_resid, &rr_spmv))) return rc;
+                S1.spmv += rr_spmv;
+            }
+        }
+    }
+    if (fp32 && accepted) {
+        S = p.hs;
+        S.spmv = S1.spmv;
+    } else if (fp32) {
         fp64_phase_start(p, E.stream);
         State S0 = initial_state(nev, ncv, o);
         p.hs = S0;
@@ -1024,7 +1159,21 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
         S.napply += S1.napply;
     }
     int status = map_status(S.status);
-    if (S.status == ST_CONVERGED) {
+    if (S.status == ST_CONVERGED && accepted) {
+        // the refined pairs are in the library's vout and SM_VALS
+        const int m = p.ncv, nconv = p.hs.nconv;
+        if (device_out) {
+            CK(cudaMemcpyAsync(values, p.small + SM_VALS(m), sizeof(double) * nconv, cudaMemcpyDeviceToDevice, E.stream));
+            CK(cudaMemcpy2DAsync(vectors, sizeof(double) * (size_t)ldv, p.vout, sizeof(double) * (size_t)p.ldo,
+                                 sizeof(double) * (size_t)n, m, cudaMemcpyDeviceToDevice, E.stream));
+        } else {
+            CK(cudaMemcpyAsync(values, p.small + SM_VALS(m), sizeof(double) * nconv, cudaMemcpyDeviceToHost, E.stream));
+            if ((rc = copy_d2h_2d(vectors, sizeof(double) * (size_t)ldv, p.vout, sizeof(double) * (size_t)p.ldo,
+                                  sizeof(double) * (size_t)n, m, E.stream)))
+                return rc;
+        }
+        CK(cudaStreamSynchronize(E.stream));
+    } else if (S.status == ST_CONVERGED) {
         if (device_out) {
             if (p.own_vout && p.vout) cudaFree(p.vout);
             p.vout = vectors;
@@ -1050,6 +1199,7 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
     }
     const double nnz = csr ? (double)csr->nnz : 0.0;
     fill_stats(stats, S, p, nnz, fp32 ? 1 : 0, refine_restarts, now_s() - t0, status);
+    if (stats) stats->refine_residual = rr_resid;
     if (stats && S.status == ST_CONVERGED) stats->bytes_restart += 16.0 * n * ncv;
     fill_profile(S, p, nnz, fp32 ? 1 : 0);
     return status;
@@ -1252,7 +1402,20 @@ int hlanc_csr_create(int dev, int nrows, int ncols, int nnz, const int *row_ptr,
         CK(cudaStreamSynchronize(h->stream));
     }
     CK(cudaStreamSynchronize(h->stream));
+    int rc = autotune_spmv(h.get(), grp);
+    if (rc) return rc;
     *out = h.release();
+    return HLANC_OK;
+}
+
+int hlanc_csr_tuning(hlanc_csr_t h, int *rows_per_unit, int *lanes4_mean, int *lanes8_mean, double *us_default,
+                     double *us_chosen) {
+    if (!h) return HLANC_ERR_INVALID;
+    if (rows_per_unit) *rows_per_unit = h->tune[0];
+    if (lanes4_mean) *lanes4_mean = h->tune[2];
+    if (lanes8_mean) *lanes8_mean = h->tune[3];
+    if (us_default) *us_default = h->tune_us_default;
+    if (us_chosen) *us_chosen = h->tune_us;
     return HLANC_OK;
 }
 

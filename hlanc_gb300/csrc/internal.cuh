@@ -79,7 +79,6 @@ struct Problem {
     const int *col;
     const double *val;
     const float *val32;    // FP32 values (mixed precision), or null
-    float *x32;            // FP32 copy of the current Lanczos vector
     int n, ld, ncv, nev0;
     int tile0, ntiles;
     int fp32;              // SpMV on FP32 values/vectors
@@ -326,6 +325,11 @@ void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, const
 void launch_gather(const Problem *P_d, int nprob, const long long *off_d, double *buf_d, cudaStream_t s);
 void launch_scatter(const Problem *P_d, int nprob, const long long *off_d, const int *flag_d,
                     const double *buf_d, cudaStream_t s);
+// FP64 Rayleigh-Ritz of a mixed-precision solve (kernels_refine.cu):
+// G = Y^T W (part: gram_blocks(n) * k * k doubles), out = Y Z.
+int gram_blocks(int n);
+void launch_gram(const double *Y, const double *W, int n, int ld, int k, double *part, double *G, cudaStream_t s);
+void launch_rotate(const double *Y, int n, int ld, int k, const double *Z, double *out, cudaStream_t s);
 void launch_residuals(const int *row_ptr, const int *col, const double *val, int n, int k,
                       const double *values_d, const double *vectors_d, int ldv, double *out4k,
                       cudaStream_t s);

@@ -66,15 +66,11 @@ __device__ __forceinline__ bool group_sync(unsigned *bar, unsigned nb, unsigned 
 }
 
 // Sum of nv value-major partials (src[i * nb + t], t < nb) into dst[i], in
-// the same order in every CTA.
+// the same order in every CTA: each warp loads 8 values' partials at once
+// (one round trip to L2 for up to 32 values per CTA) and sums them with one
+// transposed butterfly.
 __device__ __forceinline__ void reduce_all(const double *src, int nb, int nv, double *dst) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = warp; i < nv; i += CTPB / 32) {
-        double a = 0.0;
-        for (int t = lane; t < nb; t += 32) a += __ldcg(src + (size_t)i * nb + t);
-        a = warp_sum(a);
-        if (lane == 0) dst[i] = a;
-    }
+    reduce_slots(src, nb, nb, nv, dst);
     __syncthreads();
 }
 
@@ -167,21 +163,31 @@ __global__ void __launch_bounds__(CTPB) k_cycle(const Problem *__restrict__ prob
             double nrm = 0.0;
             if (pass == 1)
                 for (int r = row0 + tid; r < row1; r += CTPB) nrm = fma(w[r], w[r], nrm);
-            for (int c0 = 0; c0 < c; c0 += 8) {
-                double a[8];
+            for (int c0 = 0; c0 < c; c0 += 16) {       // two panels of 8 per round
+                double a[8], b[8];
 #pragma unroll
-                for (int q = 0; q < 8; ++q) a[q] = 0.0;
-                const int cc = min(8, c - c0);
+                for (int q = 0; q < 8; ++q) a[q] = b[q] = 0.0;
+                const int cc = min(16, c - c0);
                 for (int r = row0 + tid; r < row1; r += CTPB) {
                     const double wr = w[r];
                     const double *vr = P.V + (size_t)c0 * ld + r;
+                    double va[8], vb[8];
 #pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        if (q < cc) a[q] = fma(vr[(size_t)q * ld], wr, a[q]);
+                    for (int q = 0; q < 8; ++q) {
+                        va[q] = q < cc ? vr[(size_t)q * ld] : 0.0;
+                        vb[q] = q + 8 < cc ? vr[(size_t)(q + 8) * ld] : 0.0;
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        if (q < cc) a[q] = fma(va[q], wr, a[q]);
+                        if (q + 8 < cc) b[q] = fma(vb[q], wr, b[q]);
+                    }
                 }
                 const double v = warp_reduce8(a);
+                const double u = warp_reduce8(b);
                 const int q = lane >> 2;
                 if ((lane & 3) == 0 && q < cc) wsum[warp][c0 + q] = v;
+                if ((lane & 3) == 0 && q + 8 < cc) wsum[warp][c0 + 8 + q] = u;
             }
             if (pass == 1) {
                 nrm = warp_sum(nrm);
@@ -227,10 +233,25 @@ __global__ void __launch_bounds__(CTPB) k_cycle(const Problem *__restrict__ prob
             double nrm2 = 0.0;
             for (int r = row0 + tid; r < row1; r += CTPB) {
                 double acc = w[r];
+                // columns 8 at a time, loads issued before the FMAs
                 float a32 = 0.0f;
-                for (int i = 0; i < tf; ++i) a32 = fmaf(P.V32[(size_t)i * ld + r], h32s[i], a32);
+                for (int i0 = 0; i0 < tf; i0 += 8) {
+                    float v[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) v[q] = i0 + q < tf ? P.V32[(size_t)(i0 + q) * ld + r] : 0.0f;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (i0 + q < tf) a32 = fmaf(v[q], h32s[i0 + q], a32);
+                }
                 acc = fma(-(double)a32, unscale, acc);
-                for (int i = tf; i < c; ++i) acc = fma(-P.V[(size_t)i * ld + r], hs[i], acc);
+                for (int i0 = tf; i0 < c; i0 += 8) {
+                    double v[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) v[q] = i0 + q < c ? P.V[(size_t)(i0 + q) * ld + r] : 0.0;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (i0 + q < c) acc = fma(-v[q], hs[i0 + q], acc);
+                }
                 w[r] = acc;
                 nrm2 = fma(acc, acc, nrm2);
             }

@@ -208,17 +208,31 @@ __device__ __forceinline__ void split8(const double (&x)[8], int emax, uint4 (&p
 #pragma unroll
         for (int s = 0; s < NDIG; ++s) dg[s][e] = digit_of(lo, hi, neg, s);
     }
+    // a digit (|d| <= 255) has at most 8 significant bits, so its bf16 is the
+    // upper half of its FP32 pattern exactly: two byte permutes per pair
+    // instead of conversions (on GB300 the conversion instructions share the
+    // narrow FP64 pipe)
 #pragma unroll
     for (int s = 0; s < NDIG; ++s) {
-        __nv_bfloat162 p0 = __floats2bfloat162_rn(dg[s][0], dg[s][1]);
-        __nv_bfloat162 p1 = __floats2bfloat162_rn(dg[s][2], dg[s][3]);
-        __nv_bfloat162 p2 = __floats2bfloat162_rn(dg[s][4], dg[s][5]);
-        __nv_bfloat162 p3 = __floats2bfloat162_rn(dg[s][6], dg[s][7]);
-        planes[s].x = *reinterpret_cast<unsigned *>(&p0);
-        planes[s].y = *reinterpret_cast<unsigned *>(&p1);
-        planes[s].z = *reinterpret_cast<unsigned *>(&p2);
-        planes[s].w = *reinterpret_cast<unsigned *>(&p3);
+        planes[s].x = __byte_perm(__float_as_uint(dg[s][0]), __float_as_uint(dg[s][1]), 0x7632);
+        planes[s].y = __byte_perm(__float_as_uint(dg[s][2]), __float_as_uint(dg[s][3]), 0x7632);
+        planes[s].z = __byte_perm(__float_as_uint(dg[s][4]), __float_as_uint(dg[s][5]), 0x7632);
+        planes[s].w = __byte_perm(__float_as_uint(dg[s][6]), __float_as_uint(dg[s][7]), 0x7632);
     }
+}
+
+// The integer value of an integer-valued FP32 level (|x| < 2^31) from its
+// bit pattern, with integer instructions only (a level sum of integer
+// products is an integer: below 2^24 it is exact, above it every FP32 value
+// is an integer).
+__device__ __forceinline__ long long level_int(float f) {
+    const unsigned u = __float_as_uint(f);
+    const int e = (int)((u >> 23) & 0xFFu);
+    if (e < 127) return 0;                         // |f| < 1: zero
+    const long long m = (long long)((u & 0x7FFFFFu) | 0x800000u);
+    const int sh = e - 150;                        // |f| = m 2^sh
+    const long long v = sh >= 0 ? (m << sh) : (m >> (-sh));
+    return (u >> 31) ? -v : v;
 }
 
 // Levels D_0..D_6 (exact integers in FP32) of one output -> the FP64 value
@@ -230,10 +244,10 @@ __device__ __forceinline__ void split8(const double (&x)[8], int emax, uint4 (&p
 // A0 + B0 fits in 35 significant bits, so (A - (A0 + B0)) is exact and
 // the value costs two FP64 additions with one rounding.
 __device__ __forceinline__ double combine(const float (&d)[NDIG], int ex, int fx) {
-    // every level is an integer below 2^26 in magnitude
-    const long long l0 = __float2int_rn(d[0]), l1 = __float2int_rn(d[1]), l2 = __float2int_rn(d[2]);
-    const long long l3 = __float2int_rn(d[3]), l4 = __float2int_rn(d[4]), l5 = __float2int_rn(d[5]);
-    const long long l6 = __float2int_rn(d[6]);
+    // every level is an integer below 2^28 in magnitude
+    const long long l0 = level_int(d[0]), l1 = level_int(d[1]), l2 = level_int(d[2]);
+    const long long l3 = level_int(d[3]), l4 = level_int(d[4]), l5 = level_int(d[5]);
+    const long long l6 = level_int(d[6]);
     const long long hi = (l0 << 16) + (l1 << 8) + l2;                 // |hi| < 2^41
     const long long lo = (l3 << 24) + (l4 << 16) + (l5 << 8) + l6;    // |lo| < 2^50
     const int S = ex + fx - 2106;

@@ -119,6 +119,65 @@ int tridiag_eig(int n, double *d, double *e, double *zl, double *Z, int ldz) {
     return 0;
 }
 
+// Cyclic Jacobi for a dense symmetric matrix (Golub & Van Loan 4e,
+// Alg. 8.5.1 "symSchur2" and Alg. 8.5.3): rotations zero each off-diagonal
+// pair in turn until the off-diagonal norm is below n eps ||A||_F (the
+// rounding level of the rotations themselves).
+int sym_eig_jacobi(int n, double *A, double *w, double *Z) {
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) Z[i + (size_t)j * n] = (i == j) ? 1.0 : 0.0;
+    double fro = 0.0;
+    for (int i = 0; i < n * n; ++i) fro += A[i] * A[i];
+    fro = sqrt(fro);
+    const double eps = DBL_EPSILON * 0.5;
+    int ok = 0;
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0.0;
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i < n; ++i)
+                if (i != j) off += A[i + (size_t)j * n] * A[i + (size_t)j * n];
+        if (sqrt(off) <= n * eps * fro || fro == 0.0) { ok = 1; break; }
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[p + (size_t)q * n];
+                if (apq == 0.0) continue;
+                const double tau = (A[q + (size_t)q * n] - A[p + (size_t)p * n]) / (2.0 * apq);
+                const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                const double c = 1.0 / sqrt(1.0 + t * t), sn = t * c;
+                for (int k = 0; k < n; ++k) {           // A <- A J (columns p, q)
+                    const double akp = A[k + (size_t)p * n], akq = A[k + (size_t)q * n];
+                    A[k + (size_t)p * n] = c * akp - sn * akq;
+                    A[k + (size_t)q * n] = sn * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {           // A <- J^T A (rows p, q)
+                    const double apk = A[p + (size_t)k * n], aqk = A[q + (size_t)k * n];
+                    A[p + (size_t)k * n] = c * apk - sn * aqk;
+                    A[q + (size_t)k * n] = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {           // Z <- Z J
+                    const double zkp = Z[k + (size_t)p * n], zkq = Z[k + (size_t)q * n];
+                    Z[k + (size_t)p * n] = c * zkp - sn * zkq;
+                    Z[k + (size_t)q * n] = sn * zkp + c * zkq;
+                }
+            }
+    }
+    for (int i = 0; i < n; ++i) w[i] = A[i + (size_t)i * n];
+    for (int i = 0; i < n - 1; ++i) {             // ascending, columns of Z alike
+        int k = i;
+        for (int j = i + 1; j < n; ++j)
+            if (w[j] < w[k]) k = j;
+        if (k != i) {
+            const double t = w[i]; w[i] = w[k]; w[k] = t;
+            for (int r = 0; r < n; ++r) {
+                const double tz = Z[r + (size_t)i * n];
+                Z[r + (size_t)i * n] = Z[r + (size_t)k * n];
+                Z[r + (size_t)k * n] = tz;
+            }
+        }
+    }
+    return ok ? 0 : 1;
+}
+
 // dsgets (HLanc.hpp:1387-1401), stable insertion sorts.
 static void dsgets(int nev, int np, double *ritz, double *bounds) {
     const int m = nev + np;

@@ -38,5 +38,10 @@ int finalize(FinalizeIO &io);
 // Symmetric tridiagonal eigensolver (implicit QR, Wilkinson shift).
 int tridiag_eig(int n, double *d, double *e, double *zl, double *Z, int ldz);
 
+// Dense symmetric eigensolver (cyclic Jacobi): A (n x n, column-major) is
+// destroyed; w receives the eigenvalues ascending, Z (n x n) the
+// eigenvectors as columns.  0 on success, 1 if the sweeps did not converge.
+int sym_eig_jacobi(int n, double *A, double *w, double *Z);
+
 }  // namespace host
 }  // namespace hlanc

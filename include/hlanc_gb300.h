@@ -35,7 +35,10 @@ extern "C" {
 
 /* ---- precision modes --------------------------------------------------- */
 #define HLANC_PREC_FP64           0  /* FP64 SpMV (the reference's arithmetic) */
-#define HLANC_PREC_FP32_REFINE    1  /* FP32 SpMV, FP64 everywhere else, FP64 refinement */
+#define HLANC_PREC_FP32_REFINE    1  /* FP32 SpMV, FP64 everywhere else, FP64 refinement: a
+                                        Rayleigh-Ritz of the FP32 phase's pairs with the FP64
+                                        operator, accepted when every FP64 residual meets tol,
+                                        else FP64 restart cycles from the refined vectors */
 
 /* Kernel of the restart's basis update V <- V Q (hlanc_opts_t.basis_kernel). */
 #define HLANC_BASIS_AUTO          0  /* tensor cores (FP64-accurate integer splitting) when
@@ -110,6 +113,14 @@ int hlanc_csr_apply(hlanc_csr_t op, const double *x, double *y);
 int hlanc_csr_spmv_async(hlanc_csr_t op, const double *x_d, double *y_d, void *stream);
 /* FP32 SpMV (values rounded to FP32, FP32 accumulation per row). */
 int hlanc_csr_spmv_f32_async(hlanc_csr_t op, const float *x_d, float *y_d, void *stream);
+/* The SpMV work units hlanc_csr_create picked for this matrix (no reference
+ * counterpart).  A matrix of >= 2^16 rows with rows longer than 12 entries
+ * is tuned on the device: a few unit shapes (rows per unit, mean row lengths
+ * at which a unit takes 4 / 8 lanes per row) are timed and the fastest is
+ * kept; us_default / us_chosen are the measured SpMV times (0 when the row
+ * histogram left nothing to choose). */
+int hlanc_csr_tuning(hlanc_csr_t op, int *rows_per_unit, int *lanes4_mean, int *lanes8_mean, double *us_default,
+                     double *us_chosen);
 
 /* ---- solver (ds_solver_gpu, HLanc.hpp:1868-1872 / ds_solver, 1650-1850) - */
 /* Host operator callback: y = A x for host vectors of length n; return 0 on
@@ -152,7 +163,10 @@ typedef struct {
     double bytes_cgs;         /* algorithmic bytes moved, CGS passes */
     double bytes_restart;     /* algorithmic bytes moved, basis updates + Ritz vectors */
     double cgs_update_fp32_share;  /* share of the CGS update's columns read from the FP32 copy */
-    double reserved[3];
+    double refine_residual;   /* mixed precision: largest ||A y - theta y|| / ||A||_inf after the
+                                 FP64 Rayleigh-Ritz of the FP32 phase's pairs (-1: not run); the
+                                 pairs were accepted as they are when refine_restarts == 0 */
+    double reserved[2];
 } hlanc_stats_t;
 
 /* ds_solver_gpu(n, nev, ncv, values, vectors, ldv, op, dev): largest

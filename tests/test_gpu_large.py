@@ -95,6 +95,18 @@ def test_default_large_path_matches_reference(H, case, gen, nev, ncv, mixed):
     assert used["basis_tc"] > 0 and used["basis_fp64"] == 0, used
 
 
+@pytest.mark.parametrize("case,gen,nev,ncv", CASES)
+def test_spmv_units_tuned_from_row_histogram(H, case, gen, nev, ncv):
+    """Uneven rows (the power-law graph) are tuned on the device; uniform
+    short rows (the Laplacian) keep the default units untimed."""
+    m = gen()
+    t = H.dcsrmv_operator_gpu(m).tuning()
+    if case.startswith("chunglu"):
+        assert t["us_default"] > 0 and 0 < t["us_chosen"] <= t["us_default"], t
+    else:
+        assert t["us_default"] == 0 and t["rows_per_unit"] == 1024, t
+
+
 @pytest.mark.parametrize("case,gen,nev,ncv", CASES[:1])
 def test_all_fp64_kernels_match_reference_at_large_n(H, case, gen, nev, ncv):
     g = golden(f"{case}.npz")
@@ -119,6 +131,5 @@ def test_full_size_workloads_match_reference(H, case, gen, nev, ncv):
     m = gen()
     _check_matrix(g, m)
     _solve_and_check(H, g, m, nev, ncv, H.HLANC_PREC_FP64)
-    if case.startswith("c3"):
-        op32 = None  # noqa: F841 - mixed mode is the workload's own precision
+    if case.startswith("c3"):      # the power-law workload's own precision mode too
         _solve_and_check(H, g, m, nev, ncv, H.HLANC_PREC_FP32_REFINE)
