@@ -2,12 +2,13 @@
 # Build the reference's own CPU solver (HLanc.hpp, unmodified) into
 # oracle/_ref/libhlanc_ref.so.  Checker only: used in the development
 # container to pin the oracle restatement and to write tests/golden/.
-# Needs the reference sources (HLANC_REFERENCE, default /root/reference),
+# Needs the reference sources (HLANC_REFERENCE, else a directory named
+# reference beside the repository),
 # nvcc (the header defines two __global__ kernels) and scipy's bundled
 # OpenBLAS as the MKL stand-in (oracle/ref_shim/mkl.h).
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${HLANC_REFERENCE:-/root/reference}
+REF=${HLANC_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}
 if [ ! -f "$REF/HLanc.hpp" ]; then
     echo "build_ref: reference sources not found at $REF; skipping" >&2
     exit 0

@@ -4,11 +4,12 @@
 # unmodified, against this repository's include/HLanc.hpp and libhlanc_gb300.
 # The demos include "../HLanc.hpp"; they are built in a scratch tree ($1)
 # whose HLanc.hpp includes this repository's header.  Exit 3 when the
-# reference sources are absent (HLANC_REFERENCE, default /root/reference).
+# reference sources are absent (HLANC_REFERENCE, else a directory named
+# reference beside the repository).
 set -e
 OUT=$1
-REF=${HLANC_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")/../.." && pwd)
+REF=${HLANC_REFERENCE:-$(dirname "$HERE")/reference}
 [ -d "$REF/demo" ] || { echo "reference demos not found at $REF" >&2; exit 3; }
 mkdir -p "$OUT/demo"
 echo "#include \"$HERE/include/HLanc.hpp\"" > "$OUT/HLanc.hpp"
