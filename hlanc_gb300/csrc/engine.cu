@@ -20,7 +20,10 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <condition_variable>
+#include <functional>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/HLanc.hpp"
@@ -47,6 +50,95 @@ static void report_cuda_error(cudaError_t e, const char *what, const char *file,
 static double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
+
+// ---- host worker pool ------------------------------------------------------------
+// The O(ncv^2) restart math of a batch or a serving lane is one independent
+// host routine per problem (a 24-column restart takes ~50 us on one core,
+// so 512 problems would hold one core for ~25 ms per cycle).  They run on a
+// few worker threads, started on first use and joined at exit; each problem
+// writes only its own host mirror, so the result does not depend on which
+// thread ran it.  A second caller that finds the pool busy runs its loop
+// inline.
+class HostPool {
+public:
+    static HostPool &get() {
+        static HostPool pool;
+        return pool;
+    }
+    // fn(i) for i in [0, count); returns when all are done.
+    void run(int count, const std::function<void(int)> &fn) {
+        std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
+        if (count < 4 || !busy.owns_lock() || !start()) {
+            for (int i = 0; i < count; ++i) fn(i);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            fn_.store(&fn);
+            count_.store(count);
+            next_.store(0);
+            done_ = 0;
+            ++gen_;
+        }
+        cv_.notify_all();
+        const int mine = work();
+        std::unique_lock<std::mutex> g(mu_);
+        done_ += mine;
+        done_cv_.wait(g, [&] { return done_ == count_.load(); });
+        fn_.store(nullptr);
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+            ++gen_;
+        }
+        cv_.notify_all();
+        for (auto &t : threads_) t.join();
+    }
+
+private:
+    bool start() {
+        if (started_) return !threads_.empty();
+        started_ = true;
+        const unsigned hc = std::thread::hardware_concurrency();
+        const int nw = (int)std::min(15u, hc > 1 ? hc - 1 : 0u);
+        for (int i = 0; i < nw; ++i) threads_.emplace_back([this] { loop(); });
+        return !threads_.empty();
+    }
+    int work() {
+        int n = 0;
+        for (int i = next_.fetch_add(1); i < count_.load(); i = next_.fetch_add(1)) {
+            (*fn_.load())(i);
+            ++n;
+        }
+        return n;
+    }
+    void loop() {
+        unsigned long long seen = 0;
+        for (;;) {
+            {
+                std::unique_lock<std::mutex> g(mu_);
+                cv_.wait(g, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                if (!fn_.load()) continue;
+            }
+            const int n = work();
+            std::lock_guard<std::mutex> g(mu_);
+            done_ += n;
+            if (done_ == count_.load()) done_cv_.notify_all();
+        }
+    }
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    std::vector<std::thread> threads_;
+    std::atomic<const std::function<void(int)> *> fn_{nullptr};
+    std::atomic<int> count_{0}, next_{0};
+    int done_ = 0;
+    unsigned long long gen_ = 0;
+    bool stop_ = false, started_ = false;
+};
 
 // ---- device CSR operator --------------------------------------------------------
 struct hlanc_csr_s {
@@ -787,6 +879,27 @@ public:
     void host_restarts(int *running, int *nev_max, int *np_max) {
         *running = 0; *nev_max = 0; *np_max = 0;
         const double t0 = now_s();
+        // the problems due for a restart, computed on the host pool
+        std::vector<int> due;
+        std::vector<host::RestartIO> ios;
+        std::vector<int> rss;
+        if (!device_restart) {
+            for (size_t a = 0; a < active.size(); ++a) {
+                const ProbRes &p = probs[active[a]];
+                const State &S = p.hs;
+                if (S.status != ST_RUNNING || S.phase != PH_EXTEND || S.iter < 0) continue;
+                host::RestartIO io;
+                io.ncv = p.ncv; io.nev0 = S.nev0; io.np0 = S.np0; io.max_iter = S.max_iter;
+                io.tol = S.tol; io.eps23 = S.eps23; io.rnorm = S.rnorm; io.iter = S.iter;
+                io.h = probs[active[a]].h.data(); io.ritz_s = probs[active[a]].ritz_s.data();
+                io.bnds_s = probs[active[a]].bnds_s.data(); io.Q = probs[active[a]].Q.data();
+                due.push_back((int)a);
+                ios.push_back(io);
+            }
+            rss.assign(due.size(), 0);
+            HostPool::get().run((int)due.size(), [&](int i) { rss[i] = host::restart(ios[i]); });
+        }
+        size_t q = 0;
         for (size_t a = 0; a < active.size(); ++a) {
             ProbRes &p = probs[active[a]];
             flag_h[a] = 0;
@@ -799,12 +912,10 @@ public:
                 }
                 continue;
             }
-            if (S.status != ST_RUNNING || S.phase != PH_EXTEND || S.iter < 0) continue;
-            host::RestartIO io;
-            io.ncv = p.ncv; io.nev0 = S.nev0; io.np0 = S.np0; io.max_iter = S.max_iter;
-            io.tol = S.tol; io.eps23 = S.eps23; io.rnorm = S.rnorm; io.iter = S.iter;
-            io.h = p.h.data(); io.ritz_s = p.ritz_s.data(); io.bnds_s = p.bnds_s.data(); io.Q = p.Q.data();
-            const int rs = host::restart(io);
+            if (q >= due.size() || due[q] != (int)a) continue;
+            const host::RestartIO &io = ios[q];
+            const int rs = rss[q];
+            ++q;
             S.iter = io.iter;
             S.nconv = io.nconv;
             double *slot = mbox_h + off_h[a];
@@ -846,19 +957,27 @@ public:
             launch_finalize(P_d, (int)active.size(), max_ncv, stream);
         } else {
             for (size_t q = 0; q < active.size(); ++q) flag_h[q] = 0;
-            for (int prob : which) {
-                ProbRes &p = probs[prob];
-                const int a = slot_of(prob);
-                State &S = p.hs;
-                if (S.status != ST_CONVERGED) continue;
+            std::vector<int> conv;
+            for (int prob : which)
+                if (probs[prob].hs.status == ST_CONVERGED) conv.push_back(prob);
+            std::vector<int> frc(conv.size(), 0);
+            HostPool::get().run((int)conv.size(), [&](int i) {
+                ProbRes &p = probs[conv[i]];
+                const State &S = p.hs;
                 host::FinalizeIO io;
                 io.ncv = p.ncv; io.nev0 = S.nev0; io.np0 = S.np0; io.nconv = S.nconv;
                 io.tol = S.tol; io.eps23 = S.eps23;
                 io.h = p.h.data(); io.ritz_s = p.ritz_s.data(); io.bnds_s = p.bnds_s.data();
                 io.values = p.values.data();
+                io.Q2 = mbox_h + off_h[slot_of(conv[i])] + MBOX_STATE + 2 * p.ncv;
+                frc[i] = host::finalize(io);
+            });
+            for (size_t i = 0; i < conv.size(); ++i) {
+                ProbRes &p = probs[conv[i]];
+                const int a = slot_of(conv[i]);
+                State &S = p.hs;
                 double *slot = mbox_h + off_h[a];
-                io.Q2 = slot + MBOX_STATE + 2 * p.ncv;
-                if (host::finalize(io)) {
+                if (frc[i]) {
                     S.status = ST_FAILED;
                     S.fin = 2;
                     flag_h[a] = 2;
