@@ -474,6 +474,7 @@ public:
     // one-launch extensions (kernels_cycle.cu): CTA table, barrier counters
     CycTileH *C_d = nullptr;
     unsigned *bars_d = nullptr;
+    double *xpart_d = nullptr;           // nctas_cap x (MAXNCV + 2) partial sums
     int nctas = 0, nctas_cap = 0;
     long long rows_active = 0;           // rows of all problems in the launch tables
     Problem one_h;                       // descriptor of a single-problem launch table
@@ -508,6 +509,7 @@ public:
         if (S_d) cudaFree(S_d);
         if (C_d) cudaFree(C_d);
         if (bars_d) cudaFree(bars_d);
+        if (xpart_d) cudaFree(xpart_d);
         if (off_d) cudaFree(off_d);
         if (flag_d) cudaFree(flag_d);
         if (mbox_d) cudaFree(mbox_d);
@@ -606,6 +608,9 @@ public:
             if (C_d) cudaFree(C_d);
             nctas_cap = (int)C.size() + 64;
             CK(cudaMalloc(&C_d, sizeof(CycTileH) * nctas_cap));
+            if (xpart_d) cudaFree(xpart_d);
+            xpart_d = nullptr;
+            CK(cudaMalloc(&xpart_d, sizeof(double) * (MAXNCV + 2) * (size_t)nctas_cap));
         }
         if (!bars_d || nslots_cap > bars_cap) {
             if (bars_d) cudaFree(bars_d);
@@ -622,7 +627,7 @@ public:
     // launches of launch_step.
     void enqueue_steps(int steps) {
         if (nctas > 0) {
-            (void)launch_cycle(P_d, C_d, nctas, bars_d, (int)active.size(), steps, stream);
+            (void)launch_cycle(P_d, C_d, nctas, bars_d, xpart_d, (int)active.size(), steps, stream);
             return;
         }
         for (int s = 0; s < steps; ++s)

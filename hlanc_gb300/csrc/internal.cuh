@@ -336,12 +336,13 @@ void launch_residuals(const int *row_ptr, const int *col, const double *val, int
 
 // Whole Lanczos extensions in one cooperative launch (kernels_cycle.cu):
 // tiles_d holds one CycTile per CTA (problem slot, rank in its group, group
-// size, rows); bars_d one barrier counter per problem slot, zeroed here.
+// size, rows); bars_d one barrier counter per problem slot, zeroed here;
+// xpart_d nctas x (MAXNCV + 2) doubles of partial sums.
 int cycle_capacity();
 int cycle_rows_per_cta();
 struct CycTileH { int prob, rank, nb, row0, row1, pad; };
-cudaError_t launch_cycle(const Problem *P_d, const void *tiles_d, int nctas, unsigned *bars_d, int nprob, int steps,
-                         cudaStream_t s);
+cudaError_t launch_cycle(const Problem *P_d, const void *tiles_d, int nctas, unsigned *bars_d, double *xpart_d,
+                         int nprob, int steps, cudaStream_t s);
 
 // Kernels this library launched (all host threads), and launches per
 // kernel variant (HLANC_KL_*).
