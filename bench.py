@@ -343,31 +343,41 @@ def batch_problems(count, seed=3):
     return [G.banded_random(int(n), int(b), seed=seed, problem=i) for i, (n, b) in enumerate(zip(ns, bws))]
 
 
-def serve_requests(count, seed=4, rate=200.0, n_lo=1000, n_hi=2000000):
-    """Poisson request stream: exponential inter-arrival times (mean 1/rate)
-    from seed, n log-uniform in [n_lo, n_hi], generator uniform over the
-    workloads' families, nev uniform in {4, 8, 16}, ncv = 3 nev, 70% FP32-SpMV
-    + refinement and 30% plain FP64.  The draws are counter-based, so the
-    first k requests of a longer stream are the same k requests."""
+def serve_draws(count, seed=4, rate=200.0, n_lo=1000, n_hi=2000000):
+    """Descriptors of the Poisson request stream: exponential inter-arrival
+    times (mean 1/rate) from seed, n log-uniform in [n_lo, n_hi], generator
+    uniform over the workloads' families, nev uniform in {4, 8, 16}, ncv =
+    3 nev, 70% FP32-SpMV + refinement and 30% plain FP64.  The draws are
+    counter-based, so the first k requests of a longer stream are the same k
+    requests."""
     u = G.uniform01(seed, 40, 6 * count).reshape(count, 6)
     arrivals = np.cumsum(-np.log(1.0 - u[:, 0]) / rate)
-    reqs = []
+    out = []
     for i in range(count):
         n = int(np.exp(np.log(n_lo) + u[i, 1] * (np.log(n_hi) - np.log(n_lo))))
-        fam = int(u[i, 2] * 4)
-        if fam == 0:
-            nx = max(int(round(np.sqrt(n))), 8)
-            m = G.laplacian_2d(nx)
-        elif fam == 1:
-            N = max(int(round(n ** (1 / 3))), 6)
-            m = G.laplacian_3d(N, shift_seed=seed + i)
-        elif fam == 2:
-            m = G.banded_random(n, 2 + int(u[i, 5] * 15), seed=seed, problem=1000 + i)
-        else:
-            m = G.chung_lu_normalized(max(n, 1024), seed=seed + i)
         nev = (4, 8, 16)[min(int(u[i, 3] * 3), 2)]
-        mixed = u[i, 4] < 0.7
-        reqs.append(dict(t=float(arrivals[i]), m=m, nev=nev, ncv=3 * nev, mixed=bool(mixed), fam=fam))
+        out.append(dict(i=i, seed=seed, t=float(arrivals[i]), n=n, fam=int(u[i, 2] * 4), bw=2 + int(u[i, 5] * 15),
+                        nev=nev, ncv=3 * nev, mixed=bool(u[i, 4] < 0.7)))
+    return out
+
+
+def serve_matrix(d):
+    """The matrix of one request descriptor (serve_draws)."""
+    n, fam, seed, i = d["n"], d["fam"], d["seed"], d["i"]
+    if fam == 0:
+        return G.laplacian_2d(max(int(round(np.sqrt(n))), 8))
+    if fam == 1:
+        return G.laplacian_3d(max(int(round(n ** (1 / 3))), 6), shift_seed=seed + i)
+    if fam == 2:
+        return G.banded_random(n, d["bw"], seed=seed, problem=1000 + i)
+    return G.chung_lu_normalized(max(n, 1024), seed=seed + i)
+
+
+def serve_requests(count, seed=4, rate=200.0, n_lo=1000, n_hi=2000000):
+    """The first `count` requests of the stream with their matrices."""
+    reqs = []
+    for d in serve_draws(count, seed, rate, n_lo, n_hi):
+        reqs.append(dict(t=d["t"], m=serve_matrix(d), nev=d["nev"], ncv=d["ncv"], mixed=d["mixed"], fam=d["fam"]))
     return reqs
 
 
@@ -503,6 +513,126 @@ def serve_compare(H, reqs, slots=32, lanes=0, arms=("server", "server_all_fp64",
     return out
 
 
+class _Feeder:
+    """Matrices of the stream, generated ahead of use in spawned worker
+    processes (at most `ahead` outstanding), in arrival order."""
+
+    def __init__(self, descs, workers, ahead):
+        import multiprocessing as mp
+        self.descs, self.ahead = descs, ahead
+        self.pool = mp.get_context("spawn").Pool(workers)
+        self.jobs, self.next = {}, 0
+        self.top_up(0)
+
+    def top_up(self, consumed):
+        while self.next < len(self.descs) and self.next - consumed < self.ahead:
+            self.jobs[self.next] = self.pool.apply_async(serve_matrix, (self.descs[self.next],))
+            self.next += 1
+
+    def ready(self, i):
+        return self.jobs[i].ready()
+
+    def take(self, i):
+        m = self.jobs.pop(i).get()
+        self.top_up(i + 1)
+        return m
+
+    def close(self):
+        self.pool.terminate()
+
+
+def serve_stream(H, count, arm, slots=32, lanes=0, workers=12, ahead=48):
+    """One arm over the first `count` requests of the stream, matrices made on
+    the fly (the stream does not fit in memory at once): "server" (continuous
+    batching), "server_all_fp64", or "plain" (the plain FP64 solver, one
+    request at a time in arrival order).  A request's operator is built when
+    it arrives and its matrix is ready, and freed when it completes;
+    latency = completion - arrival."""
+    descs = serve_draws(count)
+    feed = _Feeder(descs, workers, ahead)
+    lat, pairs, ok = [], 0, 0
+    try:
+        if arm == "plain":
+            t0 = time.perf_counter()
+            for d in descs:
+                m = feed.take(d["i"])
+                now = time.perf_counter() - t0
+                if d["t"] > now:
+                    time.sleep(d["t"] - now)
+                op = H.dcsrmv_operator_gpu(m, precision=H.HLANC_PREC_FP64)
+                rc, _, _, _ = H.solve(op, d["nev"], d["ncv"], tol=1e-10)
+                op.close()
+                lat.append(time.perf_counter() - t0 - d["t"])
+                pairs += d["nev"] if rc == 0 else 0
+                ok += rc == 0
+            eng = None
+        else:
+            srv = H.Server(mem_budget_bytes=150 << 30, max_slots=slots, lanes=lanes)
+            t0 = time.perf_counter()
+            nxt, ids, ops = 0, {}, {}
+            while len(lat) < count:
+                now = time.perf_counter() - t0
+                while nxt < count and descs[nxt]["t"] <= now and feed.ready(nxt):
+                    d = descs[nxt]
+                    mixed = d["mixed"] and arm == "server"
+                    prec = H.HLANC_PREC_FP32_REFINE if mixed else H.HLANC_PREC_FP64
+                    op = H.dcsrmv_operator_gpu(feed.take(nxt), precision=prec)
+                    ids[srv.submit(op, d["nev"], d["ncv"], tol=1e-10, precision=prec)] = nxt
+                    ops[nxt] = op
+                    nxt += 1
+                active, waiting = srv.step()
+                for rid, i in list(ids.items()):
+                    res = srv.poll(rid)
+                    if res is not None:
+                        del ids[rid]
+                        ops.pop(i).close()
+                        lat.append(time.perf_counter() - t0 - descs[i]["t"])
+                        pairs += descs[i]["nev"] if res[0] == 0 else 0
+                        ok += res[0] == 0
+                if active == 0 and waiting == 0 and nxt < count:
+                    wait = descs[nxt]["t"] - (time.perf_counter() - t0)
+                    if wait > 0:
+                        time.sleep(wait)
+                    elif not feed.ready(nxt):
+                        feed.jobs[nxt].wait(0.05)
+            eng = srv.stats()
+            srv.close()
+        t_total = time.perf_counter() - t0
+    finally:
+        feed.close()
+    la = np.sort(np.array(lat))
+    out = {"requests": len(la), "converged": ok, "seconds": t_total, "eigenpairs_per_s": pairs / t_total,
+           "p50_s": float(np.percentile(la, 50)), "p95_s": float(np.percentile(la, 95)),
+           "p99_s": float(np.percentile(la, 99))}
+    if eng is not None:
+        out["engine"] = eng
+    return out
+
+
+def run_serve_stream(args):
+    import hlanc_gb300 as H
+    from hlanc_gb300 import build
+    build.build()
+    arms = args.serve_arms.split(",")
+    out = {a: serve_stream(H, args.serve_stream, a, args.serve_slots, args.serve_lanes) for a in arms}
+    if "plain" in out:
+        for a in arms:
+            if a != "plain":
+                out[f"throughput_ratio_{a}"] = out[a]["eigenpairs_per_s"] / out["plain"]["eigenpairs_per_s"]
+                out[f"p99_ratio_plain_over_{a}"] = out["plain"]["p99_s"] / out[a]["p99_s"]
+    line = {"metric": "serving throughput (eigenpairs/s) and latency", "value": out[arms[0]]["eigenpairs_per_s"],
+            "unit": "eigenpairs/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64 (70% fp32 SpMV)",
+            "data": "synthetic (seeded generators)",
+            "config": {"workload": f"serve_stream{args.serve_stream}", "arrivals": "Poisson, mean 200 req/s, seed 4",
+                       "n": "log-uniform [1000, 2000000]", "nev": "{4,8,16}, ncv = 3 nev",
+                       "mix": "70% fp32+refine / 30% fp64", "tol": 1e-10, "max_restarts": 200,
+                       "slots": args.serve_slots, "lanes": args.serve_lanes or 2, "mem_budget_GB": 150,
+                       "stream": f"the first {args.serve_stream} requests of the seed-4 stream of 20,000",
+                       "matrices": "generated ahead of use in 12 spawned processes; operators built on arrival"},
+            **out}
+    print(json.dumps(line), flush=True)
+
+
 def c3_compare(H, m, golden):
     """The Chung-Lu graph n = 2^22 (nev 16, ncv 48) in plain FP64 and in
     mixed precision, each pair against the reference's own CPU solve."""
@@ -599,12 +729,18 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--serve-lanes", type=int, default=0, help="server launch lanes (0 = library default)")
     ap.add_argument("--serve-nmax", type=int, default=2000000, help="largest n of the request stream")
+    ap.add_argument("--serve-stream", type=int, default=0,
+                    help="serve the first N requests of the stream with matrices generated on the fly")
+    ap.add_argument("--serve-arms", default="server,plain", help="arms of --serve-stream")
     args = ap.parse_args()
     if args.batch:
         run_batch(args)
         return
     if args.serve:
         run_serve(args)
+        return
+    if args.serve_stream:
+        run_serve_stream(args)
         return
     wl = WORKLOADS[args.workload]
     m = wl["gen"]()
