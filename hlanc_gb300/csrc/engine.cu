@@ -153,8 +153,22 @@ struct hlanc_csr_s {
     long long max_row = 0;                      // longest row (entries), general CSR
     int tune[4] = {SPMV_ROWS, SPMV_NNZ, SUBWARP4_MEAN, SUBWARP8_MEAN};   // SpMV unit shape in use
     double tune_us = 0.0, tune_us_default = 0.0;   // measured SpMV time of it / of the default (0: not tuned)
+    double sell_us = 0.0;                        // measured SpMV time of the sliced-ELL candidate
     std::vector<SpmvTile> stiles_h;             // entry-balanced SpMV work units (prob = 0)
     SpmvTile *stiles_d = nullptr;
+    // sliced-ELL copy (kind 5 units) when the tuner picked it
+    long long *sl_ptr_d = nullptr;
+    int *sl_len_d = nullptr, *sl_row_d = nullptr, *sl_col_d = nullptr;
+    double *sl_val_d = nullptr;
+    float *sl_val32_d = nullptr;
+    long long sl_elems = 0;
+    Sell sell() const { return Sell{sl_ptr_d, sl_len_d, sl_row_d, sl_col_d, sl_val_d, sl_val32_d}; }
+    void free_sell() {
+        cudaFree(sl_ptr_d); cudaFree(sl_len_d); cudaFree(sl_row_d); cudaFree(sl_col_d);
+        cudaFree(sl_val_d); cudaFree(sl_val32_d);
+        sl_ptr_d = nullptr; sl_len_d = sl_row_d = sl_col_d = nullptr; sl_val_d = nullptr; sl_val32_d = nullptr;
+        sl_elems = 0;
+    }
     std::mutex mu;
 };
 
@@ -192,13 +206,97 @@ static void build_spmv_tiles(const int *rp, int nrows, std::vector<SpmvTile> &ou
     }
 }
 
+// Sliced-ELL layout of the rows of at most LONG_ROW entries (Sell,
+// internal.cuh): windows of SELL_SIGMA consecutive such rows, sorted by
+// length (longest first; a counting sort, stable) and cut into slices of
+// SELL_C rows.  Longer rows keep their 16-lanes-per-row and CTA-per-row
+// units: a lane walking one row of hundreds of entries alone (one dependent
+// gather after another) made its warp the kernel's critical path.  Only the slice
+// metadata is built here; columns and values are copied on the device.
+struct SellBuild {
+    std::vector<long long> ptr;
+    std::vector<int> len, row;
+    std::vector<SpmvTile> units;
+    long long elems = 0;
+};
+static void build_sell(const int *rp, int nrows, SellBuild &B) {
+    std::vector<int> win, cnt(LONG_ROW + 2), sorted;
+    win.reserve(SELL_SIGMA);
+    auto flush = [&]() {
+        if (win.empty()) return;
+        std::fill(cnt.begin(), cnt.end(), 0);
+        for (int r : win) ++cnt[LONG_ROW - (rp[r + 1] - rp[r])];      // longest first
+        int acc = 0;
+        for (int &c : cnt) { const int t = c; c = acc; acc += t; }
+        sorted.assign(win.size(), 0);
+        for (int r : win) sorted[cnt[LONG_ROW - (rp[r + 1] - rp[r])]++] = r;
+        const int first = (int)B.len.size();
+        for (size_t i = 0; i < sorted.size(); i += SELL_C) {
+            int mx = 0;
+            for (int l = 0; l < SELL_C; ++l) {
+                const int r = i + l < sorted.size() ? sorted[i + l] : -1;
+                B.row.push_back(r);
+                if (r >= 0) mx = std::max(mx, rp[r + 1] - rp[r]);
+            }
+            B.ptr.push_back(B.elems);
+            B.len.push_back(mx);
+            B.elems += (long long)mx * SELL_C;
+        }
+        const int last = (int)B.len.size();
+        for (int sl = first; sl < last; sl += SELL_SLICES_PER_UNIT)
+            B.units.push_back({0, sl, std::min(last, sl + SELL_SLICES_PER_UNIT), 5});
+        win.clear();
+    };
+    for (int r = 0; r < nrows;) {
+        const int l = rp[r + 1] - rp[r];
+        if (l > WIDE_ROW) {                     // whole CTA
+            B.units.push_back({0, r, r + 1, 2});
+            ++r;
+        } else if (l > LONG_ROW) {              // runs of medium rows, 16 lanes each
+            const int r0 = r;
+            while (r < nrows && r - r0 < TPB / 16 && rp[r + 1] - rp[r] > LONG_ROW && rp[r + 1] - rp[r] <= WIDE_ROW) ++r;
+            B.units.push_back({0, r0, r, 1});
+        } else {
+            win.push_back(r);
+            ++r;
+            if ((int)win.size() == SELL_SIGMA) flush();
+        }
+    }
+    flush();
+}
+
+// Device copy of a SellBuild into h (columns and values from h's CSR).
+static int upload_sell(hlanc_csr_s *h, const SellBuild &B) {
+    cudaStream_t s = h->stream;
+    const size_t ns = B.len.size();
+    const size_t ne = (size_t)std::max<long long>(B.elems, 1);
+    CK(cudaMalloc(&h->sl_ptr_d, sizeof(long long) * std::max<size_t>(ns, 1)));
+    CK(cudaMalloc(&h->sl_len_d, sizeof(int) * std::max<size_t>(ns, 1)));
+    CK(cudaMalloc(&h->sl_row_d, sizeof(int) * std::max<size_t>(B.row.size(), 1)));
+    CK(cudaMalloc(&h->sl_col_d, sizeof(int) * ne));
+    CK(cudaMalloc(&h->sl_val_d, sizeof(double) * ne));
+    if (h->val32_d) CK(cudaMalloc(&h->sl_val32_d, sizeof(float) * ne));
+    h->sl_elems = B.elems;
+    if (ns) {
+        CK(cudaMemcpyAsync(h->sl_ptr_d, B.ptr.data(), sizeof(long long) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(h->sl_len_d, B.len.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(h->sl_row_d, B.row.data(), sizeof(int) * B.row.size(), cudaMemcpyHostToDevice, s));
+        launch_sell_fill(h->rp_d, h->ci_d, h->val_d, (int)ns, h->sl_ptr_d, h->sl_len_d, h->sl_row_d, h->sl_col_d,
+                         h->sl_val_d, h->sl_val32_d, s);
+        CK(cudaGetLastError());
+    }
+    return HLANC_OK;
+}
+
 // SpMV units tuned per matrix.  The row-length histogram decides whether
 // there is anything to choose: when no row has more than SUBWARP4_MEAN
 // entries, every short unit runs thread per row whatever the thresholds and
 // the default units stand (the Laplacians).  Otherwise a few unit shapes --
 // rows per unit and the mean row lengths at which a unit takes 4 / 8 lanes
 // per row -- are built and each SpMV is timed on the device (one warm-up,
-// best of three, CUDA events), and the fastest is kept.  Problems of fewer
+// best of three, CUDA events), and the fastest is kept.  The sliced-ELL
+// layout (build_sell) is one more candidate, kept (a second copy of the
+// matrix, with its padding) only when it is the fastest.  Problems of fewer
 // than 2^16 rows keep the default: their SpMV is launch-latency bound.
 static int autotune_spmv(hlanc_csr_s *h, const int *grp) {
     if (h->nrows < (1 << 16) || h->max_row <= SUBWARP4_MEAN) return HLANC_OK;
@@ -220,18 +318,27 @@ static int autotune_spmv(hlanc_csr_s *h, const int *grp) {
         build_spmv_tiles(grp, h->nrows, tiles[c], cand[c]);
         cap = std::max(cap, tiles[c].size());
     }
+    SellBuild sb;
+    build_sell(grp, h->nrows, sb);
+    tiles.push_back(sb.units);
+    cap = std::max(cap, sb.units.size());
     CK(cudaMalloc(&r.t, sizeof(SpmvTile) * std::max<size_t>(cap, 1)));
+    if (int rc = upload_sell(h, sb)) {
+        h->free_sell();
+        return rc;
+    }
+    const Sell sl = h->sell();
     int best = 0;
-    std::vector<double> us(nc, 0.0);
-    for (int c = 0; c < nc; ++c) {
+    std::vector<double> us(nc + 1, 0.0);
+    for (int c = 0; c <= nc; ++c) {
         const int nt = (int)tiles[c].size();
         if (!nt) continue;
         CK(cudaMemcpyAsync(r.t, tiles[c].data(), sizeof(SpmvTile) * nt, cudaMemcpyHostToDevice, s));
-        launch_spmv(h->rp_d, h->ci_d, h->val_d, r.t, nt, h->xs_d, h->ys_d, s);
+        launch_spmv(h->rp_d, h->ci_d, h->val_d, sl, r.t, nt, h->xs_d, h->ys_d, s);
         float bestms = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
             CK(cudaEventRecord(r.e0, s));
-            launch_spmv(h->rp_d, h->ci_d, h->val_d, r.t, nt, h->xs_d, h->ys_d, s);
+            launch_spmv(h->rp_d, h->ci_d, h->val_d, sl, r.t, nt, h->xs_d, h->ys_d, s);
             CK(cudaEventRecord(r.e1, s));
             CK(cudaEventSynchronize(r.e1));
             float ms = 0.f;
@@ -243,7 +350,15 @@ static int autotune_spmv(hlanc_csr_s *h, const int *grp) {
     }
     h->tune_us_default = us[0];
     h->tune_us = us[best];
-    h->tune[0] = cand[best].rows; h->tune[1] = cand[best].nnz; h->tune[2] = cand[best].sub4; h->tune[3] = cand[best].sub8;
+    h->sell_us = us[nc];
+    if (best == nc) {
+        h->tune[0] = -1; h->tune[1] = 0; h->tune[2] = 0; h->tune[3] = 0;
+    } else {
+        h->tune[0] = cand[best].rows; h->tune[1] = cand[best].nnz; h->tune[2] = cand[best].sub4;
+        h->tune[3] = cand[best].sub8;
+        CK(cudaStreamSynchronize(s));
+        h->free_sell();
+    }
     if (best != 0) {
         h->stiles_h.swap(tiles[best]);
         CK(cudaFree(h->stiles_d));
@@ -651,6 +766,7 @@ public:
             if (p.csr) {
                 q.row_ptr = p.csr->rp_d; q.col = p.csr->ci_d; q.val = p.csr->val_d;
                 q.val32 = p.fp32 ? p.csr->val32_d : nullptr;
+                q.sell = p.csr->sell();
             }
             q.n = p.n; q.ld = p.ld; q.ncv = p.ncv; q.nev0 = p.nev0;
             q.tile0 = (int)T.size(); q.ntiles = p.ntiles;
@@ -1182,7 +1298,8 @@ int refine_rr(Engine &E, ProbRes &p, double tol, bool *accepted, double *resid_m
     double *G = t.small, *Zd = G + k * k, *th = Zd + k * k, *out4 = th + k;
     const int nst = (int)c->stiles_h.size();
     for (int i = 0; i < k; ++i)
-        launch_spmv(c->rp_d, c->ci_d, c->val_d, c->stiles_d, nst, p.vout + (size_t)i * ldo, t.W + (size_t)i * ldo, s);
+        launch_spmv(c->rp_d, c->ci_d, c->val_d, c->sell(), c->stiles_d, nst, p.vout + (size_t)i * ldo,
+                    t.W + (size_t)i * ldo, s);
     launch_gram(p.vout, t.W, n, ldo, k, t.part, G, s);
     std::vector<double> g((size_t)k * k), z((size_t)k * k), w(k), r4(4 * (size_t)k);
     CK(cudaMemcpyAsync(g.data(), G, sizeof(double) * k * k, cudaMemcpyDeviceToHost, s));
@@ -1551,6 +1668,7 @@ int hlanc_csr_destroy(hlanc_csr_t h) {
         if (h->val32_d) cudaFree(h->val32_d);
         cudaFree(h->xs_d); cudaFree(h->ys_d);
         if (h->stiles_d) cudaFree(h->stiles_d);
+        h->free_sell();
         if (h->stream) cudaStreamDestroy(h->stream);
     }
     delete h;
@@ -1598,7 +1716,7 @@ int hlanc_csr_apply(hlanc_csr_t h, const double *x, double *y) {
         xx = h->xs_d;
     }
     if (!is_device_ptr(y, h->dev)) yy = h->ys_d;
-    launch_spmv(h->rp_d, h->ci_d, h->val_d, h->stiles_d, (int)h->stiles_h.size(), xx, yy, h->stream);
+    launch_spmv(h->rp_d, h->ci_d, h->val_d, h->sell(), h->stiles_d, (int)h->stiles_h.size(), xx, yy, h->stream);
     CK(cudaGetLastError());
     if (yy != y) CK(cudaMemcpyAsync(y, yy, sizeof(double) * h->nrows, cudaMemcpyDefault, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -1608,7 +1726,8 @@ int hlanc_csr_apply(hlanc_csr_t h, const double *x, double *y) {
 int hlanc_csr_spmv_async(hlanc_csr_t h, const double *x_d, double *y_d, void *stream) {
     if (!h || !x_d || !y_d) return HLANC_ERR_INVALID;
     DevGuard g(h->dev);
-    launch_spmv(h->rp_d, h->ci_d, h->val_d, h->stiles_d, (int)h->stiles_h.size(), x_d, y_d, (cudaStream_t)stream);
+    launch_spmv(h->rp_d, h->ci_d, h->val_d, h->sell(), h->stiles_d, (int)h->stiles_h.size(), x_d, y_d,
+                (cudaStream_t)stream);
     CK(cudaGetLastError());
     return HLANC_OK;
 }
@@ -1617,7 +1736,7 @@ int hlanc_csr_spmv_f32_async(hlanc_csr_t h, const float *x_d, float *y_d, void *
     if (!h || !x_d || !y_d) return HLANC_ERR_INVALID;
     if (!h->val32_d) return HLANC_ERR_INVALID;
     DevGuard g(h->dev);
-    launch_spmv_f32(h->rp_d, h->ci_d, h->val32_d, h->stiles_d, (int)h->stiles_h.size(), x_d, y_d,
+    launch_spmv_f32(h->rp_d, h->ci_d, h->val32_d, h->sell(), h->stiles_d, (int)h->stiles_h.size(), x_d, y_d,
                     (cudaStream_t)stream);
     CK(cudaGetLastError());
     return HLANC_OK;

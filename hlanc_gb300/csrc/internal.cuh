@@ -73,6 +73,25 @@ __host__ __device__ inline int SM_Q(int m)      { return 12 * m; }      // m*m (
 __host__ __device__ inline int SM_Q2(int m)     { return 12 * m + m * m; }  // m*m (final Householder Q)
 __host__ __device__ inline int SM_SIZE(int m)   { return 12 * m + 2 * m * m; }
 
+// Sliced-ELL copy of a matrix's rows of at most LONG_ROW entries (kind 5
+// units; row0/row1 are slice indices, SELL_SLICES_PER_UNIT slices per
+// unit).  Rows are sorted by length inside windows of SELL_SIGMA rows and
+// packed SELL_C to a slice; element k of lane l of slice s sits at
+// ptr[s] + k * SELL_C + l (padding: column 0, value 0), so a warp walks
+// 32 rows of nearly equal length with coalesced loads and every FP64 FMA
+// slot does useful work.  row[s * SELL_C + l] is the lane's row (-1: none).
+constexpr int SELL_C = 32;
+constexpr int SELL_SIGMA = 1024;
+constexpr int SELL_SLICES_PER_UNIT = 8;   // = TPB / 32: one warp per slice
+struct Sell {
+    const long long *ptr;
+    const int *len;
+    const int *row;
+    const int *col;
+    const double *val;
+    const float *val32;
+};
+
 struct Problem {
     // operator (general CSR on the device)
     const int *row_ptr;
@@ -94,6 +113,7 @@ struct Problem {
     const double *wext;    // non-null: operator output is supplied by the host callback path
     double *vout;          // Ritz vectors destination (device, ldo x ncv)
     int ldo, pad2;
+    Sell sell;             // sliced-ELL rows of the operator (kind 5 SpMV units), or null pointers
 };
 
 struct Tile { int prob, row0, row1, pad; };
@@ -121,6 +141,7 @@ constexpr int WIDE_ROW = 2048;
 constexpr int SUBWARP4_MEAN = 12;
 constexpr int SUBWARP8_MEAN = 32;
 struct SpmvTile { int prob, row0, row1, kind; };
+
 
 // ---- device helpers --------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
@@ -318,10 +339,15 @@ bool basis_tc_fits(int max_ncv, int nev_max);
 void launch_basis_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, int nev_max, cudaStream_t s);
 void launch_finalize(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
 void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, cudaStream_t s);
-void launch_spmv(const int *row_ptr, const int *col, const double *val, const SpmvTile *stiles, int nstiles,
-                 const double *x, double *y, cudaStream_t s);
-void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, const SpmvTile *stiles,
+void launch_spmv(const int *row_ptr, const int *col, const double *val, const Sell &sell, const SpmvTile *stiles,
+                 int nstiles, const double *x, double *y, cudaStream_t s);
+void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, const Sell &sell, const SpmvTile *stiles,
                      int nstiles, const float *x, float *y, cudaStream_t s);
+// Fill the sliced-ELL arrays (col, val, val32 may be null) of nslices
+// slices from the general CSR, given ptr / len / row.
+void launch_sell_fill(const int *row_ptr, const int *col, const double *val, int nslices, const long long *ptr,
+                      const int *len, const int *row, int *out_col, double *out_val, float *out_val32,
+                      cudaStream_t s);
 void launch_gather(const Problem *P_d, int nprob, const long long *off_d, double *buf_d, cudaStream_t s);
 void launch_scatter(const Problem *P_d, int nprob, const long long *off_d, const int *flag_d,
                     const double *buf_d, cudaStream_t s);

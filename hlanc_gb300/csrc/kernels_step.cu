@@ -154,12 +154,53 @@ __device__ __forceinline__ T spmv_wide(const int *__restrict__ rp, const int *__
     return sum;
 }
 
+// Sliced-ELL unit (kind 5): warp w takes slice s0 + w, lane l its row; the
+// row's entries are summed in their CSR order (each FMA predicated on the
+// row's own length, so padding adds nothing, whatever x holds), and the
+// entries of four k are loaded before their FMAs.
+template <typename T, typename XL, typename Emit>
+__device__ __forceinline__ void spmv_slices(const Sell &S, const T *__restrict__ sval, const int *__restrict__ rp,
+                                            int s0, int s1, XL x, Emit emit) {
+    const int s = s0 + (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (s >= s1) return;
+    const long long base = S.ptr[s];
+    const int len = S.len[s];
+    const int row = S.row[(size_t)s * SELL_C + lane];
+    const int rl = row >= 0 ? rp[row + 1] - rp[row] : 0;
+    const int *__restrict__ c = S.col + base + lane;
+    const T *__restrict__ v = sval + base + lane;
+    T acc = T(0);
+    int k = 0;
+    for (; k + 4 <= len; k += 4) {
+        int cc[4];
+        T vv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            cc[q] = c[(size_t)(k + q) * SELL_C];
+            vv[q] = v[(size_t)(k + q) * SELL_C];
+        }
+        T xx[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) xx[q] = x(cc[q]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (k + q < rl) acc = fma(vv[q], xx[q], acc);
+    }
+    for (; k < len; ++k) {
+        const T xv = x(c[(size_t)k * SELL_C]);
+        if (k < rl) acc = fma(v[(size_t)k * SELL_C], xv, acc);
+    }
+    if (row >= 0) emit(row, acc);
+}
+
 // x: a functor giving x[c] (a plain load, or a conversion on the fly).
 template <typename T, typename XL, typename Emit>
 __device__ __forceinline__ void spmv_unit(const SpmvTile &t, const int *__restrict__ rp, const int *__restrict__ ci,
-                                          const T *__restrict__ val, XL x, int *s_col,
-                                          T *s_val, T *red, Emit emit) {
-    if (t.kind == 0) {
+                                          const T *__restrict__ val, const Sell &sell, const T *__restrict__ sval,
+                                          XL x, int *s_col, T *s_val, T *red, Emit emit) {
+    if (t.kind == 5) {
+        spmv_slices<T>(sell, sval, rp, t.row0, t.row1, x, emit);
+    } else if (t.kind == 0) {
         spmv_short<T>(rp, ci, val, x, t.row0, t.row1, s_col, s_val, emit);
     } else if (t.kind == 3) {
         spmv_subwarp<T, 4>(rp, ci, val, x, t.row0, t.row1, emit);
@@ -219,12 +260,13 @@ __global__ void __launch_bounds__(TPB, F32 ? 5 : SPMV_CTAS_PER_SM) k_spmv_step(c
         // conversions off GB300's narrow FP64 pipe.
         (void)vj;
         (void)vj32;
-        spmv_unit<float>(t, P.row_ptr, P.col, P.val32, XLoad<float>{vj32}, s_col, s_val, red,
+        spmv_unit<float>(t, P.row_ptr, P.col, P.val32, P.sell, P.sell.val32, XLoad<float>{vj32}, s_col, s_val, red,
                          [=](int rr, float acc) { w[rr] = (double)acc; });
     } else {
         // each row is emitted once: V[:, j] is written there too, instead of
         // in a separate pass over the unit's rows before the gathers start
-        spmv_unit<double>(t, P.row_ptr, P.col, P.val, XLoad<double>{rin}, s_col, s_val, red, [=](int rr, double acc) {
+        spmv_unit<double>(t, P.row_ptr, P.col, P.val, P.sell, P.sell.val, XLoad<double>{rin}, s_col, s_val, red,
+                          [=](int rr, double acc) {
             const double x = rin[rr];
             const double v = scale ? x * t1 : x;
             w[rr] = scale ? acc * t1 : acc;
@@ -679,14 +721,16 @@ __global__ void __launch_bounds__(TPB, ONE ? 6 : 5) k_apply(const Problem *__res
 template <typename T>
 __global__ void __launch_bounds__(TPB, SPMV_CTAS_PER_SM) k_spmv_plain(const int *__restrict__ rp,
                                                     const int *__restrict__ ci,
-                                                    const T *__restrict__ val,
+                                                    const T *__restrict__ val, const Sell sell,
+                                                    const T *__restrict__ sval,
                                                     const SpmvTile *__restrict__ tiles, int ntiles,
                                                     const T *__restrict__ x, T *__restrict__ y) {
     __shared__ int s_col[(TPB / 32) * STAGE];
     __shared__ T s_val[(TPB / 32) * STAGE];
     __shared__ T red[TPB / 32];
     for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x)
-        spmv_unit<T>(tiles[ti], rp, ci, val, XLoad<T>{x}, s_col, s_val, red, [=](int rr, T acc) { y[rr] = acc; });
+        spmv_unit<T>(tiles[ti], rp, ci, val, sell, sval, XLoad<T>{x}, s_col, s_val, red,
+                     [=](int rr, T acc) { y[rr] = acc; });
 }
 
 // ---- residuals of k Ritz pairs (demo/verify_eigs.cu:52-98) ------------------
@@ -844,17 +888,51 @@ void launch_cgs_kernel(const Problem *P_d, const Tile *tiles_d, int ntiles, cons
     launch_counter() += 1;
 }
 
-void launch_spmv(const int *row_ptr, const int *col, const double *val, const SpmvTile *stiles, int nstiles,
-                 const double *x, double *y, cudaStream_t s) {
+void launch_spmv(const int *row_ptr, const int *col, const double *val, const Sell &sell, const SpmvTile *stiles,
+                 int nstiles, const double *x, double *y, cudaStream_t s) {
     if (nstiles <= 0) return;
-    k_spmv_plain<double><<<spmv_grid(nstiles), TPB, 0, s>>>(row_ptr, col, val, stiles, nstiles, x, y);
+    k_spmv_plain<double><<<spmv_grid(nstiles), TPB, 0, s>>>(row_ptr, col, val, sell, sell.val, stiles, nstiles, x, y);
     launch_counter() += 1;
 }
 
-void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, const SpmvTile *stiles,
+void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, const Sell &sell, const SpmvTile *stiles,
                      int nstiles, const float *x, float *y, cudaStream_t s) {
     if (nstiles <= 0) return;
-    k_spmv_plain<float><<<spmv_grid(nstiles), TPB, 0, s>>>(row_ptr, col, val, stiles, nstiles, x, y);
+    k_spmv_plain<float><<<spmv_grid(nstiles), TPB, 0, s>>>(row_ptr, col, val, sell, sell.val32, stiles, nstiles, x, y);
+    launch_counter() += 1;
+}
+
+// Sliced-ELL fill: thread (slice, lane) copies its row's entries to
+// positions ptr[s] + k * SELL_C + lane (coalesced writes across the warp)
+// and pads the slice's remaining k with column 0, value 0.
+__global__ void __launch_bounds__(TPB) k_sell_fill(const int *__restrict__ rp, const int *__restrict__ ci,
+                                                   const double *__restrict__ va, int nslices,
+                                                   const long long *__restrict__ ptr, const int *__restrict__ len,
+                                                   const int *__restrict__ row, int *__restrict__ oc,
+                                                   double *__restrict__ ov, float *__restrict__ ov32) {
+    const long long gid = (long long)blockIdx.x * TPB + threadIdx.x;
+    const int s = (int)(gid / SELL_C), lane = (int)(gid % SELL_C);
+    if (s >= nslices) return;
+    const int r = row[(size_t)s * SELL_C + lane];
+    const int a = r >= 0 ? rp[r] : 0, rl = r >= 0 ? rp[r + 1] - a : 0;
+    const long long base = ptr[s] + lane;
+    for (int k = 0; k < len[s]; ++k) {
+        const long long o = base + (long long)k * SELL_C;
+        const bool in = k < rl;
+        const double v = in ? va[a + k] : 0.0;
+        if (oc) oc[o] = in ? ci[a + k] : 0;
+        if (ov) ov[o] = v;
+        if (ov32) ov32[o] = (float)v;
+    }
+}
+
+void launch_sell_fill(const int *row_ptr, const int *col, const double *val, int nslices, const long long *ptr,
+                      const int *len, const int *row, int *out_col, double *out_val, float *out_val32,
+                      cudaStream_t s) {
+    if (nslices <= 0) return;
+    const long long threads = (long long)nslices * SELL_C;
+    k_sell_fill<<<(unsigned)((threads + TPB - 1) / TPB), TPB, 0, s>>>(row_ptr, col, val, nslices, ptr, len, row,
+                                                                    out_col, out_val, out_val32);
     launch_counter() += 1;
 }
 

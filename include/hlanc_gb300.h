@@ -116,7 +116,9 @@ int hlanc_csr_spmv_f32_async(hlanc_csr_t op, const float *x_d, float *y_d, void 
 /* The SpMV work units hlanc_csr_create picked for this matrix (no reference
  * counterpart).  A matrix of >= 2^16 rows with rows longer than 12 entries
  * is tuned on the device: a few unit shapes (rows per unit, mean row lengths
- * at which a unit takes 4 / 8 lanes per row) are timed and the fastest is
+ * at which a unit takes 4 / 8 lanes per row) and a sliced-ELL copy of the
+ * matrix (rows sorted by length inside windows of 1024 rows, 32 rows per
+ * warp; *rows_per_unit = -1 when it was kept) are timed and the fastest is
  * kept; us_default / us_chosen are the measured SpMV times (0 when the row
  * histogram left nothing to choose). */
 int hlanc_csr_tuning(hlanc_csr_t op, int *rows_per_unit, int *lanes4_mean, int *lanes8_mean, double *us_default,

@@ -107,6 +107,34 @@ def test_spmv_units_tuned_from_row_histogram(H, case, gen, nev, ncv):
         assert t["us_default"] == 0 and t["rows_per_unit"] == 1024, t
 
 
+@pytest.mark.parametrize("gen", [lambda: G.chung_lu_normalized(1 << 18, seed=2),
+                                 lambda: G.banded_random(1 << 17, 12, seed=3, problem=9)])
+def test_tuned_spmv_layout_matches_scipy(H, gen):
+    """Whichever layout the tuner keeps for an uneven matrix (row-class units
+    or the sliced-ELL copy), y = A x agrees with scipy's product to FP64
+    rounding (|y - Ax| <= 1e-13 |A||x| per row), and the FP32 SpMV within
+    the worst-case FP32 bound (row length + 2) 2^-24 |A||x|."""
+    import torch
+    m = gen()
+    A = G.to_scipy(m)
+    x = np.random.default_rng(1).uniform(-1.0, 1.0, m.n)
+    ref = A @ x
+    scale = abs(A) @ np.abs(x)
+    op = H.dcsrmv_operator_gpu(m, precision=H.HLANC_PREC_FP32_REFINE)
+    t = op.tuning()
+    assert t["us_chosen"] > 0, t
+    y = np.zeros(m.n)
+    op(x, y)
+    assert np.all(np.abs(y - ref) <= 1e-13 * scale), (t, float(np.max(np.abs(y - ref) / scale)))
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    yd = torch.zeros(m.n, dtype=torch.float32, device="cuda")
+    H.lib().hlanc_csr_spmv_f32_async(op.handle, xd.data_ptr(), yd.data_ptr(), None)
+    torch.cuda.synchronize()
+    y32 = yd.cpu().numpy().astype(np.float64)
+    rl = np.diff(A.indptr).astype(np.float64)
+    assert np.all(np.abs(y32 - ref) <= (rl + 2.0) * 2.0 ** -24 * scale + 1e-30), t
+
+
 @pytest.mark.parametrize("case,gen,nev,ncv", CASES[:1])
 def test_all_fp64_kernels_match_reference_at_large_n(H, case, gen, nev, ncv):
     g = golden(f"{case}.npz")
