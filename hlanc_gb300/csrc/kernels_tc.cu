@@ -33,6 +33,8 @@
 // accumulators (7 x NPAD columns) in tensor memory.  One CTA per tile of
 // rows, one CTA per SM.  Measured on GB300 at n = 4.1M, ncv = 60: 2.7 ms
 // (nev 20) and 3.8 ms (nev 40) against 8.8 / 17.8 ms for the FP64 kernel.
+// k_basis_tc2 (below) runs the same products with the phases of
+// consecutive blocks overlapped by warp role, for nev + 1 <= 32.
 //
 // The same splitting was tried for the CGS passes (w -= V h, h = V^T w),
 // where each element of V meets a single output: the splitting alone costs
@@ -120,6 +122,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *m, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// The same test, with the thread suspended until the phase completes or
+// about `ns` nanoseconds pass (a waiting warp then issues nothing, instead
+// of spinning on the test and taking issue slots from the working warps).
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *m, uint32_t parity, uint32_t ns) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(m)), "r"(parity), "r"(ns)
+        : "memory");
+    return ok != 0;
+}
 // Levels 0..6 of 4 consecutive outputs of this thread's TMEM lane: seven
 // 32x32b.x4 loads (level L at column offset L * npad) and one wait, in one
 // asm block so the registers are read only after the wait.
@@ -172,19 +187,26 @@ __device__ __forceinline__ int exp_field(double x) {
 }
 
 // |X| = (mantissa << 2) >> (emax - e) < 2^55 of one element, relative to the
-// largest biased exponent emax of its row / column, as two words, and its sign.
+// largest biased exponent emax of its row / column, as two words, and its
+// sign.  32-bit funnel shifts on the two halves of the mantissa (a 64-bit
+// variable shift costs several instructions more per element).
 __device__ __forceinline__ void split_mag(double x, int emax, unsigned &lo, unsigned &hi, bool &neg) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const int ex = (int)((bits >> 52) & 0x7FF);
-    unsigned long long mag = 0ull;
+    const unsigned bh = (unsigned)__double2hiint(x), bl = (unsigned)__double2loint(x);
+    const int ex = (int)((bh >> 20) & 0x7FFu);
+    neg = (bh >> 31) != 0u;
+    const unsigned mh = (((bh & 0xFFFFFu) | 0x100000u) << 2) | (bl >> 30);   // bits 32..54 of mantissa << 2
+    const unsigned ml = bl << 2;
+    const int sh = emax - ex;
+    lo = 0u;
+    hi = 0u;
     if (ex != 0) {
-        const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
-        const int sh = emax - ex;
-        mag = sh < 64 ? (mant << 2) >> sh : 0ull;
+        if (sh < 32) {
+            lo = __funnelshift_r(ml, mh, (unsigned)sh);
+            hi = mh >> sh;
+        } else if (sh < 64) {
+            lo = mh >> (sh - 32);
+        }
     }
-    lo = (unsigned)mag;
-    hi = (unsigned)(mag >> 32);
-    neg = (bits >> 63) != 0ull;
 }
 
 // Digit s (0 = most significant) of |X| with the element's sign, as a float:
@@ -221,18 +243,18 @@ __device__ __forceinline__ void split8(const double (&x)[8], int emax, uint4 (&p
     }
 }
 
-// The integer value of an integer-valued FP32 level (|x| < 2^31) from its
-// bit pattern, with integer instructions only (a level sum of integer
-// products is an integer: below 2^24 it is exact, above it every FP32 value
-// is an integer).
+// The integer value of an integer-valued FP32 level (|x| < 2^25: at most 7
+// digit-pair sums of 64 products below 2^16) from its bit pattern, with
+// 32-bit integer instructions only (a level sum of integer products is an
+// integer: below 2^24 it is exact, above it every FP32 value is an integer).
 __device__ __forceinline__ long long level_int(float f) {
     const unsigned u = __float_as_uint(f);
     const int e = (int)((u >> 23) & 0xFFu);
     if (e < 127) return 0;                         // |f| < 1: zero
-    const long long m = (long long)((u & 0x7FFFFFu) | 0x800000u);
-    const int sh = e - 150;                        // |f| = m 2^sh
-    const long long v = sh >= 0 ? (m << sh) : (m >> (-sh));
-    return (u >> 31) ? -v : v;
+    const int m = (int)((u & 0x7FFFFFu) | 0x800000u);
+    const int sh = e - 150;                        // |f| = m 2^sh, sh <= 1
+    const int v = sh >= 0 ? (m << sh) : (m >> (-sh));
+    return (long long)((u >> 31) ? -v : v);
 }
 
 // Levels D_0..D_6 (exact integers in FP32) of one output -> the FP64 value
@@ -244,7 +266,7 @@ __device__ __forceinline__ long long level_int(float f) {
 // A0 + B0 fits in 35 significant bits, so (A - (A0 + B0)) is exact and
 // the value costs two FP64 additions with one rounding.
 __device__ __forceinline__ double combine(const float (&d)[NDIG], int ex, int fx) {
-    // every level is an integer below 2^28 in magnitude
+    // every level is an integer below 2^25 in magnitude
     const long long l0 = level_int(d[0]), l1 = level_int(d[1]), l2 = level_int(d[2]);
     const long long l3 = level_int(d[3]), l4 = level_int(d[4]), l5 = level_int(d[5]);
     const long long l6 = level_int(d[6]);
@@ -429,7 +451,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
         {
             bool done = false;
             for (unsigned spins = 0; spins < wait_limit; ++spins)
-                if (mbar_try_wait(&s_mbar, phase)) { done = true; break; }
+                if (mbar_try_wait_sleep(&s_mbar, phase, 1000u)) { done = true; break; }
             if (!done) {
                 s_fail = 1;
                 for (unsigned spins = 0; spins < (unsigned)WAIT_LIMIT_DEFAULT; ++spins)
@@ -501,6 +523,364 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
     }
 }
 
+// ---- warp-specialised form (nev + 1 <= 32) ---------------------------------
+// The same products with the phases of consecutive 128-row blocks
+// overlapped, instead of run one after another by every thread:
+//   warp 16, one thread: bulk copies (cp.async.bulk, one per column) of a
+//       block of V into a raw FP64 stage, and the MMAs;
+//   warps 0-7, splitters, two threads per row: the row's exponent, then the
+//       digit planes of each K half (columns 0-31, 32-63) into that half's
+//       A buffer as soon as the previous block's MMAs of the half have read
+//       it; the stage is released after the first half, so the next block's
+//       copy runs while the second half is split;
+//   warps 8-15, recombiners: levels from one of two TMEM accumulators while
+//       the next block's MMAs fill the other, recombination and stores.
+// mbarriers carry the hand-offs.  Every wait is bounded: one that gives up
+// raises s_fail, which the other roles' waits also watch, so every thread
+// reaches the end, where the MMAs and bulk copies in flight are drained
+// before TMEM and shared memory are released.
+namespace tc2 {
+constexpr int THREADS = 17 * 32;
+constexpr int SPLIT_WARPS = 8, REC_WARPS = 8, CTRL_WARP = 16;
+constexpr int KH = 32;                                      // columns per K half
+constexpr size_t APLANE = (size_t)tc::BM * KH * 2;          // one digit plane of one half
+constexpr size_t ABUF = (size_t)tc::NDIG * APLANE;          // one half's planes (56 KB)
+constexpr size_t STAGE = (size_t)tc::BM * tc::KMAX * 8;     // raw FP64 rows of one block (64 KB)
+}  // namespace tc2
+
+template <int NPAD>
+static size_t basis_tc2_smem() {
+    return 2 * tc2::ABUF + (size_t)tc::NDIG * NPAD * tc::KMAX * 2 + tc2::STAGE;
+}
+
+namespace tc {
+__device__ __forceinline__ void mbar_arrive(uint64_t *m) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(m)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *m, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes)
+                 : "memory");
+}
+// One bulk copy global -> shared (16-byte aligned addresses, size a
+// multiple of 16) completing bytes on mbarrier m.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *m) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(m))
+                 : "memory");
+}
+// Bounded wait for the phase of parity `parity`: false after `limit` polls
+// (raising *fail) or as soon as another role raised *fail.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *m, uint32_t parity, unsigned limit, volatile int *fail) {
+    for (unsigned spins = 0; spins < limit; ++spins) {
+        if (mbar_try_wait_sleep(m, parity, 1000u)) return true;
+        if (*fail) return false;
+    }
+    *fail = 1;
+    return false;
+}
+// The 7 digit planes of 8 elements, stored plane by plane (few live registers).
+__device__ __forceinline__ void split8_store(const double (&x)[8], int emax, unsigned char *base, uint32_t off) {
+    unsigned lo[8], hi[8];
+    bool ng[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) split_mag(x[e], emax, lo[e], hi[e], ng[e]);
+#pragma unroll
+    for (int q = 0; q < NDIG; ++q) {
+        float d[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) d[e] = digit_of(lo[e], hi[e], ng[e], q);
+        uint4 w;
+        w.x = __byte_perm(__float_as_uint(d[0]), __float_as_uint(d[1]), 0x7632);
+        w.y = __byte_perm(__float_as_uint(d[2]), __float_as_uint(d[3]), 0x7632);
+        w.z = __byte_perm(__float_as_uint(d[4]), __float_as_uint(d[5]), 0x7632);
+        w.w = __byte_perm(__float_as_uint(d[6]), __float_as_uint(d[7]), 0x7632);
+        *reinterpret_cast<uint4 *>(base + q * tc2::APLANE + off) = w;
+    }
+}
+}  // namespace tc
+
+template <int NPAD>
+__global__ void __launch_bounds__(tc2::THREADS, 1) k_basis_tc2(const Problem *__restrict__ probs,
+                                                              const Tile *__restrict__ tiles) {
+    using namespace tc;
+    const Tile t = tiles[blockIdx.x];
+    const Problem &P = probs[t.prob];
+    State *S = P.st;
+    if (S->status != ST_RUNNING || S->phase != PH_APPLY) return;
+    const int m = P.ncv, nev = S->nev, np = S->np;
+    const int wl = S->wait_limit;
+    const unsigned limit = wl == 0 ? (unsigned)WAIT_LIMIT_DEFAULT : (wl < 0 ? 0u : (unsigned)wl);
+    const int kpad = (m + 15) & ~15;
+    const int ksteps = kpad / 16;                           // K = 16 per MMA
+    const int nout = nev + 1;
+    constexpr uint32_t ACC = (uint32_t)(NDIG * NPAD);       // columns of one accumulator
+    constexpr uint32_t NCOLS = 2 * ACC > 256 ? 512u : 256u;
+    const size_t ld = (size_t)P.ld;
+    const int nblk = (t.row1 - t.row0 + BM - 1) / BM;
+
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *sA = smem;                                               // 2 halves x 7 planes
+    unsigned char *sB = smem + 2 * tc2::ABUF;                               // 7 x NPAD x kpad
+    double *stage = reinterpret_cast<double *>(sB + (size_t)NDIG * NPAD * KMAX * 2);   // [column][128 rows]
+    __shared__ uint64_t bar_full, bar_empty, bar_afull[2], bar_aempty[2], bar_accfull[2], bar_accempty[2];
+    __shared__ uint64_t bar_drain;
+    __shared__ uint32_t s_taddr;
+    __shared__ int s_rowexp[4][BM];
+    __shared__ int s_colexp[NPAD];
+    __shared__ double s_red[32], s_mine[1], s_tot[1];
+    __shared__ int s_fail;
+    volatile int *fail = &s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const double *Q = P.small + SM_Q(m);
+    const double *h = P.small + SM_H(m);
+
+    if (warp == tc2::CTRL_WARP) {
+        tmem_alloc(&s_taddr, NCOLS);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        s_fail = 0;
+        mbar_init(&bar_full, 1);
+        mbar_init(&bar_empty, tc2::SPLIT_WARPS);
+        mbar_init(&bar_drain, 1);
+        for (int q = 0; q < 2; ++q) {
+            mbar_init(&bar_afull[q], tc2::SPLIT_WARPS);
+            mbar_init(&bar_aempty[q], 1);
+            mbar_init(&bar_accfull[q], 1);
+            mbar_init(&bar_accempty[q], tc2::REC_WARPS);
+        }
+    }
+    for (int i = tid; i < NPAD; i += tc2::THREADS) s_colexp[i] = 0;
+    __syncthreads();
+
+    // ---- B planes: the output columns of Q, split per column (as k_basis_tc) ----
+    auto qval = [&](int k, int i) -> double {
+        if (i > nev || k >= m) return 0.0;
+        if (i < nev && k > i + np) return 0.0;
+        return Q[k + (size_t)i * m];
+    };
+    const int kg = kpad >> 3;
+    for (int it = tid; it < NPAD * kg; it += tc2::THREADS) {
+        const int i = it / kg, g = it % kg;
+        int emax = 0;
+        for (int e = 0; e < 8; ++e) emax = max(emax, exp_field(qval(8 * g + e, i)));
+        atomicMax(&s_colexp[i], emax);
+    }
+    __syncthreads();
+    const size_t bplane = (size_t)NPAD * kpad * 2;
+    for (int it = tid; it < NPAD * kg; it += tc2::THREADS) {
+        const int i = it / kg, g = it % kg;
+        double x[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) x[e] = qval(8 * g + e, i);
+        uint4 pl[NDIG];
+        split8(x, s_colexp[i], pl);
+        const uint32_t off = kmajor_off(i, 8 * g, kpad);
+#pragma unroll
+        for (int q = 0; q < NDIG; ++q) *reinterpret_cast<uint4 *>(sB + q * bplane + off) = pl[q];
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    const uint32_t taddr = s_taddr;
+    double nrm = 0.0;
+
+    // Waits are taken by lane 0 and broadcast, so a warp's lanes always agree
+    // on whether to go on (a failed wait then exits the whole warp's loop).
+    auto wait0 = [&](uint64_t *bar, uint32_t par) -> bool {
+        int ok = 1;
+        if (lane == 0) ok = mbar_wait_bounded(bar, par, limit, fail) ? 1 : 0;
+        return __shfl_sync(0xffffffffu, ok, 0) != 0;
+    };
+    if (warp == tc2::CTRL_WARP) {
+        // ---------------- bulk copies (whole warp) and MMAs (lane 0) ----------------
+        if (lane == 0) fence_after();
+        int loads = 0;                          // blocks whose copies were issued
+        auto issue_load = [&](int b) {
+            const int R0 = t.row0 + b * BM;
+            const int rows = min(BM, ((t.row1 - R0) + 1) & ~1);   // even: 16-byte multiple
+            const uint32_t bytes = (uint32_t)rows * 8u;
+            if (lane == 0) mbar_expect_tx(&bar_full, bytes * (uint32_t)m);
+            __syncwarp();
+            for (int k = lane; k < m; k += 32)
+                bulk_g2s(stage + (size_t)k * BM, P.V + R0 + (size_t)k * ld, bytes, &bar_full);
+            loads = b + 1;
+        };
+        const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
+        const uint32_t sboB = (uint32_t)kg * 128u, sboA = (uint32_t)(tc2::KH / 8) * 128u;
+        auto mma_half = [&](int hh, uint32_t dacc) {
+            const int k0 = 2 * hh, k1 = min(ksteps, 2 * hh + 2);
+            for (int q = 0; q < NDIG; ++q) {
+                const uint32_t id = instr_desc(BM, (NDIG - q) * NPAD);
+                const uint32_t d = dacc + (uint32_t)(q * NPAD);
+                for (int kk = k0; kk < k1; ++kk) {
+                    const uint64_t ad = smem_desc(a0 + (uint32_t)(hh * tc2::ABUF + q * tc2::APLANE) +
+                                                      (uint32_t)(kk - k0) * 256u, 128u, sboA);
+                    mma(d, ad, smem_desc(b0 + (uint32_t)kk * 256u, 128u, sboB), id, (q | kk) ? 1u : 0u);
+                }
+            }
+        };
+        issue_load(0);
+        for (int b = 0; b < nblk; ++b) {
+            const int ab = b & 1;
+            const uint32_t dacc = taddr + (uint32_t)ab * ACC;
+            if (b >= 2 && !wait0(&bar_accempty[ab], (uint32_t)(((b >> 1) - 1) & 1))) break;
+            if (!wait0(&bar_afull[0], (uint32_t)(b & 1))) break;
+            if (lane == 0) {
+                fence_after();
+                mma_half(0, dacc);
+                mma_commit(&bar_aempty[0]);
+            }
+            __syncwarp();
+            if (b + 1 < nblk) {                 // stage released after the first half's split
+                if (!wait0(&bar_empty, (uint32_t)(b & 1))) break;
+                issue_load(b + 1);
+            }
+            if (!wait0(&bar_afull[1], (uint32_t)(b & 1))) break;
+            if (lane == 0) {
+                fence_after();
+                mma_half(1, dacc);
+                mma_commit(&bar_aempty[1]);
+                mma_commit(&bar_accfull[ab]);
+            }
+            __syncwarp();
+        }
+        // drain: the MMAs issued so far, then the last bulk copy issued
+        if (lane == 0) {
+            mma_commit(&bar_drain);
+            for (unsigned spins = 0; spins < (unsigned)WAIT_LIMIT_DEFAULT; ++spins)
+                if (mbar_try_wait(&bar_drain, 0u)) break;
+            if (loads > 0)
+                for (unsigned spins = 0; spins < (unsigned)WAIT_LIMIT_DEFAULT; ++spins)
+                    if (mbar_try_wait(&bar_full, (uint32_t)((loads - 1) & 1))) break;
+        }
+        __syncwarp();
+    } else if (warp < tc2::SPLIT_WARPS) {
+        // ---------------- splitters: two threads per row ----------------
+        const int row = tid >> 1, part = tid & 1;
+        for (int b = 0; b < nblk; ++b) {
+            const bool rok = t.row0 + b * BM + row < t.row1;
+            if (!wait0(&bar_full, (uint32_t)(b & 1))) break;
+            // exponent of the row; the second half's values stay in registers
+            double x1[2][8];
+            int emax = 0;
+#pragma unroll
+            for (int g = 0; g < 2; ++g)
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int k0 = part * 16 + g * 8 + e, k1 = tc2::KH + k0;
+                    const double v0 = (rok && k0 < m) ? stage[(size_t)k0 * BM + row] : 0.0;
+                    x1[g][e] = (rok && k1 < m) ? stage[(size_t)k1 * BM + row] : 0.0;
+                    emax = max(emax, max(exp_field(v0), exp_field(x1[g][e])));
+                }
+            emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, 1));
+            if (part == 0) s_rowexp[b & 3][row] = emax;
+            // first half, from the stage
+            if (b >= 1 && !wait0(&bar_aempty[0], (uint32_t)((b - 1) & 1))) break;
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+                double x0[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int k0 = part * 16 + g * 8 + e;
+                    x0[e] = (rok && k0 < m) ? stage[(size_t)k0 * BM + row] : 0.0;
+                }
+                split8_store(x0, emax, sA, kmajor_off(row, part * 16 + g * 8, tc2::KH));
+            }
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&bar_afull[0]);
+                mbar_arrive(&bar_empty);
+            }
+            // second half, from registers
+            if (b >= 1 && !wait0(&bar_aempty[1], (uint32_t)((b - 1) & 1))) break;
+#pragma unroll
+            for (int g = 0; g < 2; ++g)
+                split8_store(x1[g], emax, sA + tc2::ABUF, kmajor_off(row, part * 16 + g * 8, tc2::KH));
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bar_afull[1]);
+        }
+    } else {
+        // ---------------- recombiners ----------------
+        const int q4 = warp & 3, oh = (warp - tc2::SPLIT_WARPS) >> 2;
+        const int r = 32 * q4 + lane;
+        const double hn = h[nev];
+        const double qlast = Q[(m - 1) + (size_t)(nev - 1) * m];
+        const double *__restrict__ rin = (m & 1) ? P.r1 : P.r0;
+        double *__restrict__ rout = (nev & 1) ? P.r1 : P.r0;
+        for (int b = 0; b < nblk; ++b) {
+            const int ab = b & 1;
+            if (!wait0(&bar_accfull[ab], (uint32_t)((b >> 1) & 1))) break;
+            fence_after();
+            const int orow = t.row0 + b * BM + r;
+            const bool ok = orow < t.row1;
+            const int exr = s_rowexp[b & 3][r];
+            const uint32_t lane_base = taddr + ((uint32_t)(32 * q4) << 16) + (uint32_t)ab * ACC;
+            for (int c0 = 4 * oh; c0 < nout; c0 += 8) {
+                float d[NDIG][4];
+                tmem_ld_levels4(lane_base + (uint32_t)c0, (uint32_t)NPAD, d);
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int i = c0 + e;
+                    if (i >= nout || !ok) continue;
+                    float lv[NDIG];
+#pragma unroll
+                    for (int L = 0; L < NDIG; ++L) lv[L] = d[L][e];
+                    const double v = combine(lv, exr, s_colexp[i]);
+                    if (i < nev) {
+                        P.V[orow + (size_t)i * ld] = v;
+                        P.V32[orow + (size_t)i * ld] = (float)v;
+                    } else {                                      // residual (HLanc.hpp:1605-1614)
+                        double res = rin[orow] * qlast;
+                        if (hn > 0.0) res = res + hn * v;
+                        rout[orow] = res;
+                        nrm = fma(res, res, nrm);
+                    }
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bar_accempty[ab]);
+        }
+    }
+
+    // release tensor memory: the MMAs are drained (above) and every TMEM read
+    // completed before its accempty arrival
+    fence_before();
+    __syncthreads();
+    if (warp == tc2::CTRL_WARP) {
+        fence_after();
+        tmem_dealloc(taddr, NCOLS);
+    }
+    if (*fail && tid == 0) atomicExch(&S->err, DEV_ERR_MMA_WAIT);
+    nrm = block_sum0(nrm, s_red);
+    if (tid == 0) s_mine[0] = nrm;
+    __syncthreads();
+    if (!finish_tile(P, blockIdx.x - P.tile0, 1, s_mine, s_tot)) return;
+    if (tid == 0) {
+        S->rnorm = sqrt(s_tot[0]);                    // HLanc.hpp:1735
+        S->phase = PH_EXTEND;
+        S->sumnev += nev;
+        S->napply += 1;
+    }
+}
+
+template <int NPAD>
+static void basis_tc2_t(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s) {
+    static std::atomic<unsigned long long> attr{0};
+    const size_t smem = basis_tc2_smem<NPAD>();
+    smem_limit_once(k_basis_tc2<NPAD>, (int)smem, attr);
+    prof_begin(s);
+    k_basis_tc2<NPAD><<<ntiles, tc2::THREADS, smem, s>>>(P_d, tiles_d);
+    prof_end(KC_BASIS, s);
+    launch_counter() += 1;
+    variant_counter(HLANC_KL_BASIS_TC) += 1;
+}
+
 template <int NPAD>
 static size_t basis_tc_smem() {
     return (size_t)tc::NDIG * tc::BM * tc::KMAX * 2 + (size_t)tc::NDIG * NPAD * tc::KMAX * 2;
@@ -523,10 +903,12 @@ static void basis_tc_t(const Problem *P_d, const Tile *tiles_d, int ntiles, cuda
 // ..., 40, 48, 56 or 63); the caller uses k_basis otherwise.
 bool basis_tc_fits(int max_ncv, int nev_max) { return max_ncv <= tc::KMAX && nev_max + 1 <= tc::NMAX; }
 
+// Up to 32 outputs the warp-specialised kernel (two accumulators fit the
+// 512 TMEM columns); 33..64 outputs the one-phase-at-a-time kernel.
 void launch_basis_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, int nev_max, cudaStream_t s) {
     const int nout = nev_max + 1;
-    if (nout <= 16) basis_tc_t<16>(P_d, tiles_d, ntiles, s);
-    else if (nout <= 32) basis_tc_t<32>(P_d, tiles_d, ntiles, s);
+    if (nout <= 16) basis_tc2_t<16>(P_d, tiles_d, ntiles, s);
+    else if (nout <= 32) basis_tc2_t<32>(P_d, tiles_d, ntiles, s);
     else if (nout <= 48) basis_tc_t<48>(P_d, tiles_d, ntiles, s);
     else basis_tc_t<64>(P_d, tiles_d, ntiles, s);
 }
