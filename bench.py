@@ -541,64 +541,124 @@ class _Feeder:
         self.pool.terminate()
 
 
+class _OpMaker:
+    """Device operators of the stream, built ahead of use on a helper thread
+    (the C calls release the GIL, so this overlaps the solving arm), and
+    destroyed there too; the same for every arm, so the arms differ only in
+    how they solve."""
+
+    def __init__(self, H, feed, descs, prec_of, ahead=6):
+        import queue
+        import threading
+        self.H, self.feed, self.descs, self.prec_of = H, feed, descs, prec_of
+        self.ready = queue.Queue(maxsize=ahead)
+        self.done = queue.Queue()
+        self.stop = False
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+
+    def _run(self):
+        import queue
+        i = 0
+        while not self.stop:
+            try:
+                while True:
+                    self.done.get_nowait().close()
+            except queue.Empty:
+                pass
+            if i >= len(self.descs):
+                time.sleep(0.005)
+                continue
+            m = self.feed.take(i)
+            op = self.H.dcsrmv_operator_gpu(m, precision=self.prec_of(self.descs[i]))
+            while not self.stop:
+                try:
+                    self.ready.put(op, timeout=0.05)
+                    break
+                except queue.Full:
+                    try:
+                        while True:
+                            self.done.get_nowait().close()
+                    except queue.Empty:
+                        pass
+            i += 1
+
+    def close(self):
+        self.stop = True
+        self.t.join()
+        import queue
+        for q in (self.done, self.ready):
+            try:
+                while True:
+                    q.get_nowait().close()
+            except queue.Empty:
+                pass
+
+
 def serve_stream(H, count, arm, slots=32, lanes=0, workers=12, ahead=48):
     """One arm over the first `count` requests of the stream, matrices made on
     the fly (the stream does not fit in memory at once): "server" (continuous
     batching), "server_all_fp64", or "plain" (the plain FP64 solver, one
-    request at a time in arrival order).  A request's operator is built when
-    it arrives and its matrix is ready, and freed when it completes;
-    latency = completion - arrival."""
+    request at a time in arrival order).  In every arm the matrices are
+    generated ahead in spawned processes and the device operators are built
+    (and freed) on a helper thread, in arrival order; the server is handed a
+    request once it has arrived and its operator exists, keeping at most
+    slots + 16 requests submitted and unfinished (it admits in submission
+    order).  Latency = completion - arrival."""
     descs = serve_draws(count)
     feed = _Feeder(descs, workers, ahead)
+    mixed_of = lambda d: d["mixed"] and arm == "server"
+    prec_of = lambda d: H.HLANC_PREC_FP32_REFINE if mixed_of(d) else H.HLANC_PREC_FP64
+    maker = _OpMaker(H, feed, descs, prec_of)
     lat, pairs, ok = [], 0, 0
     try:
         if arm == "plain":
             t0 = time.perf_counter()
             for d in descs:
-                m = feed.take(d["i"])
+                op = maker.ready.get()
                 now = time.perf_counter() - t0
                 if d["t"] > now:
                     time.sleep(d["t"] - now)
-                op = H.dcsrmv_operator_gpu(m, precision=H.HLANC_PREC_FP64)
                 rc, _, _, _ = H.solve(op, d["nev"], d["ncv"], tol=1e-10)
-                op.close()
+                maker.done.put(op)
                 lat.append(time.perf_counter() - t0 - d["t"])
                 pairs += d["nev"] if rc == 0 else 0
                 ok += rc == 0
             eng = None
         else:
+            import queue
             srv = H.Server(mem_budget_bytes=150 << 30, max_slots=slots, lanes=lanes)
             t0 = time.perf_counter()
-            nxt, ids, ops = 0, {}, {}
+            nxt, ids, held = 0, {}, None
             while len(lat) < count:
                 now = time.perf_counter() - t0
-                while nxt < count and descs[nxt]["t"] <= now and feed.ready(nxt):
+                while nxt < count and descs[nxt]["t"] <= now and len(ids) < slots + 16:
+                    if held is None:
+                        try:
+                            held = maker.ready.get_nowait()
+                        except queue.Empty:
+                            break
                     d = descs[nxt]
-                    mixed = d["mixed"] and arm == "server"
-                    prec = H.HLANC_PREC_FP32_REFINE if mixed else H.HLANC_PREC_FP64
-                    op = H.dcsrmv_operator_gpu(feed.take(nxt), precision=prec)
-                    ids[srv.submit(op, d["nev"], d["ncv"], tol=1e-10, precision=prec)] = nxt
-                    ops[nxt] = op
+                    ids[srv.submit(held, d["nev"], d["ncv"], tol=1e-10, precision=prec_of(d))] = (nxt, held)
+                    held = None
                     nxt += 1
                 active, waiting = srv.step()
-                for rid, i in list(ids.items()):
+                for rid, (i, op) in list(ids.items()):
                     res = srv.poll(rid)
                     if res is not None:
                         del ids[rid]
-                        ops.pop(i).close()
+                        maker.done.put(op)
                         lat.append(time.perf_counter() - t0 - descs[i]["t"])
                         pairs += descs[i]["nev"] if res[0] == 0 else 0
                         ok += res[0] == 0
                 if active == 0 and waiting == 0 and nxt < count:
                     wait = descs[nxt]["t"] - (time.perf_counter() - t0)
-                    if wait > 0:
-                        time.sleep(wait)
-                    elif not feed.ready(nxt):
-                        feed.jobs[nxt].wait(0.05)
+                    time.sleep(wait if wait > 0 else 0.002)
             eng = srv.stats()
             srv.close()
         t_total = time.perf_counter() - t0
     finally:
+        maker.close()
         feed.close()
     la = np.sort(np.array(lat))
     out = {"requests": len(la), "converged": ok, "seconds": t_total, "eigenpairs_per_s": pairs / t_total,
@@ -628,7 +688,8 @@ def run_serve_stream(args):
                        "mix": "70% fp32+refine / 30% fp64", "tol": 1e-10, "max_restarts": 200,
                        "slots": args.serve_slots, "lanes": args.serve_lanes or 2, "mem_budget_GB": 150,
                        "stream": f"the first {args.serve_stream} requests of the seed-4 stream of 20,000",
-                       "matrices": "generated ahead of use in 12 spawned processes; operators built on arrival"},
+                       "matrices": "generated ahead of use in 12 spawned processes; operators built and freed "
+                                   "on a helper thread in every arm"},
             **out}
     print(json.dumps(line), flush=True)
 
