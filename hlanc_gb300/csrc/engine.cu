@@ -1178,7 +1178,7 @@ void fill_stats(hlanc_stats_t *stats, const State &S, const ProbRes &p, double n
     stats->bytes_spmv = spmv_b * (double)S.spmv;
     // projection 8 n c + 8 n; update 8 n (c - t) + 4 n t + 16 n (t columns from the FP32 copy)
     stats->bytes_cgs = 16.0 * n * (double)S.sumc - 4.0 * n * (double)S.sumt + 24.0 * n * (double)S.passes;
-    stats->bytes_restart = (8.0 * n * p.ncv + 16.0 * n) * S.napply + 8.0 * n * (double)S.sumnev;
+    stats->bytes_restart = (8.0 * n * p.ncv + 16.0 * n) * S.napply + 12.0 * n * (double)S.sumnev;
     stats->cgs_update_fp32_share = S.sumc > 0 ? (double)S.sumt / (double)S.sumc : 0.0;
     stats->refine_residual = -1.0;
 }
@@ -1201,7 +1201,7 @@ void fill_profile(const State &S, const ProbRes &p, double nnz, int fp32) {
     P.flops[KC_PROJ] = 2.0 * n * S.sumc;
     P.bytes[KC_APPLY] = 8.0 * n * (S.sumc - S.sumt) + 4.0 * n * S.sumt + 16.0 * n * S.passes;
     P.flops[KC_APPLY] = 2.0 * n * S.sumc + 2.0 * n * S.passes;
-    P.bytes[KC_BASIS] = (8.0 * n * m + 16.0 * n) * S.napply + 8.0 * n * S.sumnev;
+    P.bytes[KC_BASIS] = (8.0 * n * m + 16.0 * n) * S.napply + 12.0 * n * S.sumnev;   // V, FP32 copy
     P.flops[KC_BASIS] = 2.0 * n * m * (S.sumnev + S.napply);
     P.bytes[KC_RITZ] = 16.0 * n * m;
     P.flops[KC_RITZ] = 2.0 * n * m * m;

@@ -53,8 +53,12 @@ __device__ __forceinline__ bool group_sync(unsigned *bar, unsigned nb, unsigned 
     target += nb;
     if (threadIdx.x == 0) {
         int ok = 1;
-        __threadfence();
+        __threadfence();   // this CTA's partials (written before the __syncthreads) before its arrival
         atomicAdd(bar, 1u);
+        // The acquire loads order this CTA's later reads after the other
+        // CTAs' arrivals (and so after their fenced partials); the poll
+        // spins without sleeping, since a barrier is on the critical path
+        // of every Lanczos step.
         for (unsigned spins = 0;; ++spins) {
             if (ld_acquire(bar) >= target) break;
             if (*(volatile int *)&S->err != DEV_ERR_NONE) { ok = 0; break; }
@@ -63,9 +67,7 @@ __device__ __forceinline__ bool group_sync(unsigned *bar, unsigned nb, unsigned 
                 ok = 0;
                 break;
             }
-            __nanosleep(32);
         }
-        __threadfence();
         *s_ok = ok;
     }
     __syncthreads();
