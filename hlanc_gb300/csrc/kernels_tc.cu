@@ -4,14 +4,14 @@
 // GB300 runs FP64 FMAs at 2 per clock per SM on the CUDA cores, so the
 // FP64 form of this update (k_basis: ~nev + np FMAs per output) is
 // FP64-bound.  Here the product is computed exactly in integer arithmetic
-// on the bf16 tensor pipe (the splitting idea of Ozaki et al., "Error-free
+// on the f16 tensor pipe (the splitting idea of Ozaki et al., "Error-free
 // transformations of matrix multiplication by using fast routines of matrix
 // multiplication", Numer. Algorithms 2012):
 //
 //  * every row r of the 128-row block of V gets the exponent E_r of its
 //    largest element; each element becomes the integer |X| = |v| 2^(55-E_r)
 //    (truncated, < 2^55) with the element's sign, i.e. 7 unsigned 8-bit
-//    digits a_0 (most significant) .. a_6, each stored as a signed bf16
+//    digits a_0 (most significant) .. a_6, each stored as a signed f16
 //    (exact: |digit| <= 255 needs 8 significand bits);
 //  * every output column i of Q (the band of Q[:, i], i < nev, and the
 //    residual column Q[:, nev]) is split the same way with its own exponent;
@@ -40,7 +40,7 @@
 // where each element of V meets a single output: the splitting alone costs
 // more issue slots per element than the FP64 kernels' DFMA, so those stay
 // on the FP64 pipe.
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "internal.cuh"
 
@@ -70,9 +70,9 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
     return d;
 }
 
-// Instruction descriptor of kind::f16: D f32, A/B bf16, both K-major.
+// Instruction descriptor of kind::f16: D f32, A/B f16, both K-major.
 __host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
@@ -209,38 +209,48 @@ __device__ __forceinline__ void split_mag(double x, int emax, unsigned &lo, unsi
     }
 }
 
-// Digit s (0 = most significant) of |X| with the element's sign, as a float:
-// byte (6 - s) placed in the significand of +-(2^23 + byte), minus +-2^23.
-__device__ __forceinline__ float digit_of(unsigned lo, unsigned hi, bool neg, int s) {
-    const unsigned top = neg ? 0xCB000000u : 0x4B000000u;
-    const float c23 = neg ? -8388608.0f : 8388608.0f;
-    const unsigned word = s < 3 ? hi : lo;
-    const unsigned sel = 0x7540u | (unsigned)(s < 3 ? 2 - s : 6 - s);
-    return __uint_as_float(__byte_perm(word, top, sel)) - c23;
+// Digit plane q (0 = most significant) of 8 elements -- byte 6 - q of each
+// |X| with the element's sign -- as 4 words of f16 pairs.  A byte d becomes
+// the f16 1024 + d by placing it under the exponent of 1024 (0x64 in the
+// high byte of each half), and one f16x2 FMA per pair, (1024 + d) s -
+// 1024 s, gives s d exactly (|d| <= 255 is exact in f16): a permute, a
+// logic operation and an FMA per two digits, no conversion instruction (on
+// GB300 conversions share the narrow FP64 pipe).
+struct Signs8 {
+    unsigned sg[4], ns[4];   // per pair: (+-1, +-1) and (-+1024, -+1024) as f16x2
+};
+__device__ __forceinline__ void signs8(const bool (&ng)[8], Signs8 &S) {
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        S.sg[p] = (ng[2 * p] ? 0xBC00u : 0x3C00u) | ((ng[2 * p + 1] ? 0xBC00u : 0x3C00u) << 16);
+        S.ns[p] = (ng[2 * p] ? 0x6400u : 0xE400u) | ((ng[2 * p + 1] ? 0x6400u : 0xE400u) << 16);
+    }
+}
+__device__ __forceinline__ uint4 plane8(const unsigned (&lo)[8], const unsigned (&hi)[8], const Signs8 &S, int q) {
+    const unsigned b = (unsigned)(q < 3 ? 2 - q : 6 - q);
+    const unsigned sel = b | ((b + 4u) << 8);     // byte b of the pair's first word -> byte 0, second -> byte 2
+    unsigned w[4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        const unsigned a0 = q < 3 ? hi[2 * p] : lo[2 * p], a1 = q < 3 ? hi[2 * p + 1] : lo[2 * p + 1];
+        const unsigned t = (__byte_perm(a0, a1, sel) & 0x00FF00FFu) | 0x64006400u;
+        unsigned r;
+        asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(r) : "r"(t), "r"(S.sg[p]), "r"(S.ns[p]));
+        w[p] = r;
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-// The 7 digits of 8 elements as bf16 pairs: 7 x uint4.
+// The 7 digits of 8 elements as f16 pairs: 7 x uint4.
 __device__ __forceinline__ void split8(const double (&x)[8], int emax, uint4 (&planes)[NDIG]) {
-    float dg[NDIG][8];
+    unsigned lo[8], hi[8];
+    bool ng[8];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) {
-        unsigned lo, hi;
-        bool neg;
-        split_mag(x[e], emax, lo, hi, neg);
+    for (int e = 0; e < 8; ++e) split_mag(x[e], emax, lo[e], hi[e], ng[e]);
+    Signs8 S;
+    signs8(ng, S);
 #pragma unroll
-        for (int s = 0; s < NDIG; ++s) dg[s][e] = digit_of(lo, hi, neg, s);
-    }
-    // a digit (|d| <= 255) has at most 8 significant bits, so its bf16 is the
-    // upper half of its FP32 pattern exactly: two byte permutes per pair
-    // instead of conversions (on GB300 the conversion instructions share the
-    // narrow FP64 pipe)
-#pragma unroll
-    for (int s = 0; s < NDIG; ++s) {
-        planes[s].x = __byte_perm(__float_as_uint(dg[s][0]), __float_as_uint(dg[s][1]), 0x7632);
-        planes[s].y = __byte_perm(__float_as_uint(dg[s][2]), __float_as_uint(dg[s][3]), 0x7632);
-        planes[s].z = __byte_perm(__float_as_uint(dg[s][4]), __float_as_uint(dg[s][5]), 0x7632);
-        planes[s].w = __byte_perm(__float_as_uint(dg[s][6]), __float_as_uint(dg[s][7]), 0x7632);
-    }
+    for (int q = 0; q < NDIG; ++q) planes[q] = plane8(lo, hi, S, q);
 }
 
 // The integer value of an integer-valued FP32 level (|x| < 2^25: at most 7
@@ -304,12 +314,12 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
     constexpr uint32_t NCOLS = (NDIG * NPAD > 256) ? 512u : (NDIG * NPAD > 128 ? 256u : 128u);
 
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sA = smem;                                   // NDIG x BM x kpad bf16
+    unsigned char *sA = smem;                                   // NDIG x BM x kpad f16
     // Q's digit planes stacked: rows t * NPAD + i hold plane t of output i
     // (t = 0..6).  Plane s of V contributes to levels L = s..6 only, so its
     // MMA writes accumulator columns [s * NPAD, 7 * NPAD) with the stack's
     // first (7 - s) * NPAD rows as B: column block L meets plane L - s.
-    unsigned char *sB = smem + (size_t)NDIG * BM * KMAX * 2;    // 7 x NPAD x kpad bf16
+    unsigned char *sB = smem + (size_t)NDIG * BM * KMAX * 2;    // 7 x NPAD x kpad f16
     __shared__ uint64_t s_mbar;
     __shared__ uint32_t s_taddr;
     __shared__ int s_rowexp[NQ][BM];
@@ -585,18 +595,10 @@ __device__ __forceinline__ void split8_store(const double (&x)[8], int emax, uns
     bool ng[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) split_mag(x[e], emax, lo[e], hi[e], ng[e]);
+    Signs8 S;
+    signs8(ng, S);
 #pragma unroll
-    for (int q = 0; q < NDIG; ++q) {
-        float d[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) d[e] = digit_of(lo[e], hi[e], ng[e], q);
-        uint4 w;
-        w.x = __byte_perm(__float_as_uint(d[0]), __float_as_uint(d[1]), 0x7632);
-        w.y = __byte_perm(__float_as_uint(d[2]), __float_as_uint(d[3]), 0x7632);
-        w.z = __byte_perm(__float_as_uint(d[4]), __float_as_uint(d[5]), 0x7632);
-        w.w = __byte_perm(__float_as_uint(d[6]), __float_as_uint(d[7]), 0x7632);
-        *reinterpret_cast<uint4 *>(base + q * tc2::APLANE + off) = w;
-    }
+    for (int q = 0; q < NDIG; ++q) *reinterpret_cast<uint4 *>(base + q * tc2::APLANE + off) = plane8(lo, hi, S, q);
 }
 }  // namespace tc
 
