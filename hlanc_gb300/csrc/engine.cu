@@ -589,7 +589,7 @@ public:
     // one-launch extensions (kernels_cycle.cu): CTA table, barrier counters
     CycTileH *C_d = nullptr;
     unsigned *bars_d = nullptr;
-    double *xpart_d = nullptr;           // nctas_cap x (MAXNCV + 2) partial sums
+    double *xpart_d = nullptr;           // nctas_cap x 3 (MAXNCV + 2) partial sums
     int nctas = 0, nctas_cap = 0;
     long long rows_active = 0;           // rows of all problems in the launch tables
     Problem one_h;                       // descriptor of a single-problem launch table
@@ -725,7 +725,7 @@ public:
             CK(cudaMalloc(&C_d, sizeof(CycTileH) * nctas_cap));
             if (xpart_d) cudaFree(xpart_d);
             xpart_d = nullptr;
-            CK(cudaMalloc(&xpart_d, sizeof(double) * (MAXNCV + 2) * (size_t)nctas_cap));
+            CK(cudaMalloc(&xpart_d, sizeof(double) * 3 * (MAXNCV + 2) * (size_t)nctas_cap));
         }
         if (!bars_d || nslots_cap > bars_cap) {
             if (bars_d) cudaFree(bars_d);

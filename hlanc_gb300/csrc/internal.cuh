@@ -363,7 +363,7 @@ void launch_residuals(const int *row_ptr, const int *col, const double *val, int
 // Whole Lanczos extensions in one cooperative launch (kernels_cycle.cu):
 // tiles_d holds one CycTile per CTA (problem slot, rank in its group, group
 // size, rows); bars_d one barrier counter per problem slot, zeroed here;
-// xpart_d nctas x (MAXNCV + 2) doubles of partial sums.
+// xpart_d nctas x 3 (MAXNCV + 2) doubles of partial sums.
 int cycle_capacity();
 int cycle_rows_per_cta();
 struct CycTileH { int prob, rank, nb, row0, row1, pad; };
