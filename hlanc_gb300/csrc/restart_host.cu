@@ -49,6 +49,18 @@ static void givens(double f, double g, double &c, double &s, double &r) {
     }
 }
 
+// sqrt(a^2 + b^2): the plain formula when neither square can overflow or
+// underflow, hypot otherwise (hypot's scaling costs more than the rest of
+// a QR rotation; the tridiagonal QR is most of a host restart).
+static inline double pyth(double a, double b) {
+    const double fa = fabs(a), fb = fabs(b);
+    const double big = fa > fb ? fa : fb;
+    const double rtmin = 1.4916681462400413e-154, rtmax = 9.4807519081091774e+153;
+    if (big < rtmax && (big > rtmin || big == 0.0) && (fa > rtmin || fa == 0.0) && (fb > rtmin || fb == 0.0))
+        return sqrt(a * a + b * b);
+    return hypot(a, b);
+}
+
 // Eigenvalues (ascending) of the symmetric tridiagonal (d[n], e[n-1]);
 // zl (optional) is rotated as the last row of the eigenvector matrix, Z
 // (optional, n x n, ldz) receives all eigenvectors.  0 on success.
@@ -69,11 +81,11 @@ int tridiag_eig(int n, double *d, double *e, double *zl, double *Z, int ldz) {
         if (++iters > 30L * n) return 1;
         const double dd = 0.5 * (d[hi - 1] - d[hi]);
         const double b = e[hi - 1];
-        const double den = dd + copysign(hypot(dd, b), dd);
+        const double den = dd + copysign(pyth(dd, b), dd);
         const double mu = (den != 0.0) ? d[hi] - b * (b / den) : d[hi] - fabs(b);
         double x = d[lo] - mu, zz = e[lo];
         for (int k = lo; k < hi; ++k) {
-            const double r = hypot(x, zz);
+            const double r = pyth(x, zz);
             double c = 1.0, s = 0.0;
             if (r != 0.0) { c = x / r; s = zz / r; }
             if (k > lo) e[k - 1] = r;
