@@ -615,6 +615,7 @@ __global__ void __launch_bounds__(tc2::THREADS, 1) k_basis_tc2(const Problem *__
     const unsigned limit = wl == 0 ? (unsigned)WAIT_LIMIT_DEFAULT : (wl < 0 ? 0u : (unsigned)wl);
     const int kpad = (m + 15) & ~15;
     const int ksteps = kpad / 16;                           // K = 16 per MMA
+    const bool two = ksteps > 2;                            // ncv > 32: the second K half exists
     const int nout = nev + 1;
     constexpr uint32_t ACC = (uint32_t)(NDIG * NPAD);       // columns of one accumulator
     constexpr uint32_t NCOLS = 2 * ACC > 256 ? 512u : 256u;
@@ -740,11 +741,13 @@ __global__ void __launch_bounds__(tc2::THREADS, 1) k_basis_tc2(const Problem *__
                 if (!wait0(&bar_empty, (uint32_t)(b & 1))) break;
                 issue_load(b + 1);
             }
-            if (!wait0(&bar_afull[1], (uint32_t)(b & 1))) break;
+            if (two && !wait0(&bar_afull[1], (uint32_t)(b & 1))) break;
             if (lane == 0) {
-                fence_after();
-                mma_half(1, dacc);
-                mma_commit(&bar_aempty[1]);
+                if (two) {
+                    fence_after();
+                    mma_half(1, dacc);
+                    mma_commit(&bar_aempty[1]);
+                }
                 mma_commit(&bar_accfull[ab]);
             }
             __syncwarp();
@@ -797,7 +800,8 @@ __global__ void __launch_bounds__(tc2::THREADS, 1) k_basis_tc2(const Problem *__
                 mbar_arrive(&bar_afull[0]);
                 mbar_arrive(&bar_empty);
             }
-            // second half, from registers
+            // second half, from registers (ncv <= 32: none)
+            if (!two) continue;
             if (b >= 1 && !wait0(&bar_aempty[1], (uint32_t)((b - 1) & 1))) break;
 #pragma unroll
             for (int g = 0; g < 2; ++g)
