@@ -161,10 +161,10 @@ class ClockSampler:
 
 
 def cgs_fp64_share(kind: str, nev: int, ncv: int) -> float:
-    """Fraction of a CGS kernel's columns run as FP64 FMAs by the hybrid
-    kernels (kernels_step.cu), over the column counts c = nev+1 .. ncv of one
-    restart cycle: projection panels of 8 split 5 + 3 (tails 1,1,2,2,3,3,4 of
-    1..7), the update runs whole groups of 8 (about c/2) in FP64."""
+    """Fraction of the hybrid projection's columns run as FP64 FMAs
+    (kernels_step.cu), over the column counts c = nev+1 .. ncv of one restart
+    cycle: panels of 8 split 5 + 3 (tails 1,1,2,2,3,3,4 of 1..7).  (The
+    update's share comes from the solve's own FP32-copy column count.)"""
     tail = [0, 1, 1, 2, 2, 3, 3, 4]
     f = t = 0
     for c in range(nev + 1, ncv + 1):
