@@ -107,8 +107,20 @@ def test_spmv_units_tuned_from_row_histogram(H, case, gen, nev, ncv):
         assert t["us_default"] == 0 and t["rows_per_unit"] == 1024, t
 
 
+def _with_empty_rows(m, every=7):
+    """The matrix with every `every`-th row emptied (empty rows and uneven
+    lengths in the same sliced-ELL windows)."""
+    A = G.to_scipy(m).tolil()
+    for r in range(0, m.n, every):
+        A.rows[r] = []
+        A.data[r] = []
+    A = A.tocsr()
+    return G.CSR(m.n, m.ncols, A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data.astype(np.float64))
+
+
 @pytest.mark.parametrize("gen", [lambda: G.chung_lu_normalized(1 << 18, seed=2),
-                                 lambda: G.banded_random(1 << 17, 12, seed=3, problem=9)])
+                                 lambda: G.banded_random(1 << 17, 12, seed=3, problem=9),
+                                 lambda: _with_empty_rows(G.chung_lu_normalized(1 << 17, seed=5))])
 def test_tuned_spmv_layout_matches_scipy(H, gen):
     """Whichever layout the tuner keeps for an uneven matrix (row-class units
     or the sliced-ELL copy), y = A x agrees with scipy's product to FP64
