@@ -35,7 +35,8 @@ CGS_HYBRID_MIN_ROWS = 1 << 18     # HLANC_CGS_AUTO picks the hybrid kernels from
 HLANC_MAX_NCV = 128
 HLANC_MAX_NEV = 63
 # kernel variants counted by hlanc_kernel_launches_of
-KL_ALL, KL_PROJ_HYBRID, KL_PROJ_FP64, KL_APPLY_SHADOW, KL_APPLY_FP64, KL_BASIS_TC, KL_BASIS_FP64, KL_CYCLE = range(8)
+(KL_ALL, KL_PROJ_HYBRID, KL_PROJ_FP64, KL_APPLY_SHADOW, KL_APPLY_FP64, KL_BASIS_TC, KL_BASIS_FP64, KL_CYCLE,
+ KL_RITZ_TC, KL_RITZ_FP64) = range(10)
 HLANC_CYCLE_AUTO = 0
 HLANC_CYCLE_OFF = 1
 
@@ -435,7 +436,8 @@ def kernel_launches_of(kind: int) -> int:
 
 
 def variant_counts() -> dict:
-    names = ("all", "proj_hybrid", "proj_fp64", "apply_shadow", "apply_fp64", "basis_tc", "basis_fp64", "cycle")
+    names = ("all", "proj_hybrid", "proj_fp64", "apply_shadow", "apply_fp64", "basis_tc", "basis_fp64", "cycle",
+             "ritz_tc", "ritz_fp64")
     return {nm: kernel_launches_of(i) for i, nm in enumerate(names)}
 
 

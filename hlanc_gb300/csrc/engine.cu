@@ -1113,11 +1113,14 @@ public:
             if ((rc = push_mailbox())) return rc;
             launch_scatter(P_d, (int)active.size(), off_d, flag_d, mbox_d, stream);
         }
-        launch_ritz(P_d, T_d, ntiles, max_ncv, stream);
+        launch_ritz(P_d, T_d, ntiles, max_ncv, basis_tc, stream);
         launch_gather(P_d, (int)active.size(), off_d, mbox_d, stream);
         CK(cudaGetLastError());
         for (size_t q = 0; q < active.size(); ++q) flag_h[q] = 0;
-        return pull_mailbox(&which);
+        if ((rc = pull_mailbox(&which))) return rc;
+        for (int pi : which)   // a bounded tensor-core wait of the Ritz kernel that gave up
+            if (probs[pi].hs.err != DEV_ERR_NONE) return HLANC_ERR_DEVICE_TIMEOUT;
+        return HLANC_OK;
     }
     int finalize(int prob) { return finalize_many(std::vector<int>{prob}); }
 
@@ -2355,7 +2358,7 @@ int srv_launch(Srv &s, Srv::Lane &L) {
         r.need_norm = false;
     }
     if (norm) launch_norm_init(E.P_d, E.T_d, E.ntiles, E.stream);
-    if (ritz) launch_ritz(E.P_d, E.T_d, E.ntiles, E.max_ncv, E.stream);
+    if (ritz) launch_ritz(E.P_d, E.T_d, E.ntiles, E.max_ncv, E.basis_tc, E.stream);
     if (basis_nev > 0)
         launch_basis(E.P_d, E.T_d, E.ntiles, E.max_ncv, Engine::basis_bucket(basis_nev), E.basis_tc, E.stream);
     E.enqueue_steps(steps);

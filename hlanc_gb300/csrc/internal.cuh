@@ -338,7 +338,10 @@ bool basis_tc_fits(int max_ncv, int nev_max);
 
 void launch_basis_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, int nev_max, cudaStream_t s);
 void launch_finalize(const Problem *P_d, int nprob, int max_ncv, cudaStream_t s);
-void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, cudaStream_t s);
+void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, bool tensor_cores,
+                 cudaStream_t s);
+bool ritz_tc_fits(int max_ncv);
+void launch_ritz_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s);
 void launch_spmv(const int *row_ptr, const int *col, const double *val, const Sell &sell, const SpmvTile *stiles,
                  int nstiles, const double *x, double *y, cudaStream_t s);
 void launch_spmv_f32(const int *row_ptr, const int *col, const float *val, const Sell &sell, const SpmvTile *stiles,

@@ -12,7 +12,9 @@
 //               selected eigenvectors and the explicit orthogonal factor
 //               (HLanc.hpp:1765-1842).
 //   k_ritz      vectors = V Qfull in one pass over V (replaces the per-
-//               reflector gemv+ger of mat_v_gpu_t::dorm2r_RN, HLanc.hpp:1075-1107).
+//               reflector gemv+ger of mat_v_gpu_t::dorm2r_RN, HLanc.hpp:1075-1107)
+//               on the FP64 CUDA cores; the tensor-core form (kernels_tc.cu)
+//               is the default for ncv <= 64.
 //
 // Small dense algorithms are written from their textbook definitions:
 // tridiagonal QR with Wilkinson shift (Golub & Van Loan 4e, Alg. 8.3.2/8.3.3),
@@ -765,7 +767,14 @@ void launch_finalize(const Problem *P_d, int nprob, int, cudaStream_t s) {
     launch_counter() += 1;
 }
 
-void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, cudaStream_t s) {
+// Ritz vectors on the tensor cores (FP64-accurate digit splitting) where
+// the shape fits, else on the FP64 CUDA cores.
+void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_ncv, bool tensor_cores,
+                 cudaStream_t s) {
+    if (tensor_cores && ritz_tc_fits(max_ncv)) {
+        launch_ritz_tc(P_d, tiles_d, ntiles, s);
+        return;
+    }
     const size_t smem = sizeof(double) * (size_t)max_ncv * RITZ_PANEL;
     static std::atomic<unsigned long long> attr{0};
     smem_limit_once(k_ritz, 64 * 1024, attr);
@@ -773,6 +782,7 @@ void launch_ritz(const Problem *P_d, const Tile *tiles_d, int ntiles, int max_nc
     k_ritz<<<ntiles, TPB, smem, s>>>(P_d, tiles_d);
     prof_end(KC_RITZ, s);
     launch_counter() += 1;
+    variant_counter(HLANC_KL_RITZ_FP64) += 1;
 }
 
 }  // namespace hlanc

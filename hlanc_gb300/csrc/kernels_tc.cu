@@ -299,19 +299,24 @@ __device__ __forceinline__ double combine(const float (&d)[NDIG], int ex, int fx
 }  // namespace tc
 
 // One CTA per tile; 128-row blocks of the tile in turn.
-template <int NPAD>
+// RITZ: the same product for the Ritz vectors of a converged problem,
+// vout[:, 0:ncv) = V Q2 with the dense ncv x ncv factor Q2
+// (HLanc.hpp:1840-1843): every column of Q2 is an output, there is no
+// residual column, and nothing of the basis is overwritten.
+template <int NPAD, bool RITZ>
 __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__restrict__ probs,
                                                             const Tile *__restrict__ tiles) {
     using namespace tc;
     const Tile t = tiles[blockIdx.x];
     const Problem &P = probs[t.prob];
     State *S = P.st;
-    if (S->status != ST_RUNNING || S->phase != PH_APPLY) return;
+    if (RITZ ? (S->status != ST_CONVERGED || S->fin != 1) : (S->status != ST_RUNNING || S->phase != PH_APPLY))
+        return;
     const int m = P.ncv, nev = S->nev, np = S->np;
     const int wl = S->wait_limit;
     const unsigned wait_limit = wl == 0 ? (unsigned)WAIT_LIMIT_DEFAULT : (wl < 0 ? 0u : (unsigned)wl);
     const int kpad = (m + 15) & ~15;
-    const int nout = nev + 1;
+    const int nout = RITZ ? m : nev + 1;
     constexpr uint32_t NCOLS = (NDIG * NPAD > 256) ? 512u : (NDIG * NPAD > 128 ? 256u : 128u);
 
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -329,7 +334,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
     __shared__ int s_fail;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const double *Q = P.small + SM_Q(m);
+    const double *Q = P.small + (RITZ ? SM_Q2(m) : SM_Q(m));
     const double *h = P.small + SM_H(m);
     const size_t aplane = (size_t)BM * kpad * 2, bplane = (size_t)NPAD * kpad * 2;
 
@@ -346,10 +351,11 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
     __syncthreads();
 
     // ---- B planes: the output columns of Q, split per column -------------------
-    // column i < nev: Q[k, i] for k <= i + np (the band), i == nev: Q[:, nev]
+    // column i < nev: Q[k, i] for k <= i + np (the band), i == nev: Q[:, nev];
+    // RITZ: every column of Q2, dense
     auto qval = [&](int k, int i) -> double {
-        if (i > nev || k >= m) return 0.0;
-        if (i < nev && k > i + np) return 0.0;
+        if (i >= nout || k >= m) return 0.0;
+        if (!RITZ && i < nev && k > i + np) return 0.0;
         return Q[k + (size_t)i * m];
     };
     const int kg = kpad >> 3;
@@ -375,11 +381,11 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
 
     const uint32_t sbo = (uint32_t)kg * 128u;
     const uint32_t taddr = s_taddr;
-    const double hn = h[nev];
-    const double qlast = Q[(m - 1) + (size_t)(nev - 1) * m];
+    const double hn = RITZ ? 0.0 : h[nev];
+    const double qlast = RITZ ? 0.0 : Q[(m - 1) + (size_t)(nev - 1) * m];
     const double *__restrict__ rin = (m & 1) ? P.r1 : P.r0;
     double *__restrict__ rout = (nev & 1) ? P.r1 : P.r0;
-    const size_t ld = (size_t)P.ld;
+    const size_t ld = (size_t)P.ld, ldo = (size_t)P.ldo;
     double nrm = 0.0;
     uint32_t phase = 0;
 
@@ -495,7 +501,9 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
 #pragma unroll
                     for (int L = 0; L < NDIG; ++L) lv[L] = d[L][e];
                     const double v = combine(lv, exr, s_colexp[i]);
-                    if (i < nev) {
+                    if (RITZ) {
+                        P.vout[orow + (size_t)i * ldo] = v;
+                    } else if (i < nev) {
                         P.V[orow + (size_t)i * ld] = v;
                         P.V32[orow + (size_t)i * ld] = (float)v;
                     } else {                                      // residual (HLanc.hpp:1605-1614)
@@ -527,10 +535,14 @@ __global__ void __launch_bounds__(tc::THREADS, 1) k_basis_tc(const Problem *__re
     __syncthreads();
     if (!finish_tile(P, blockIdx.x - P.tile0, 1, s_mine, s_tot)) return;
     if (tid == 0) {
-        S->rnorm = sqrt(s_tot[0]);                    // HLanc.hpp:1735
-        S->phase = PH_EXTEND;
-        S->sumnev += nev;
-        S->napply += 1;
+        if (RITZ) {
+            S->fin = 2;
+        } else {
+            S->rnorm = sqrt(s_tot[0]);                // HLanc.hpp:1735
+            S->phase = PH_EXTEND;
+            S->sumnev += nev;
+            S->napply += 1;
+        }
     }
 }
 
@@ -897,9 +909,9 @@ template <int NPAD>
 static void basis_tc_t(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s) {
     static std::atomic<unsigned long long> attr{0};
     const size_t smem = basis_tc_smem<NPAD>();
-    smem_limit_once(k_basis_tc<NPAD>, (int)smem, attr);
+    smem_limit_once(k_basis_tc<NPAD, false>, (int)smem, attr);
     prof_begin(s);
-    k_basis_tc<NPAD><<<ntiles, tc::THREADS, smem, s>>>(P_d, tiles_d);
+    k_basis_tc<NPAD, false><<<ntiles, tc::THREADS, smem, s>>>(P_d, tiles_d);
     prof_end(KC_BASIS, s);
     launch_counter() += 1;
     variant_counter(HLANC_KL_BASIS_TC) += 1;
@@ -918,6 +930,23 @@ void launch_basis_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, int ne
     else if (nout <= 32) basis_tc2_t<32>(P_d, tiles_d, ntiles, s);
     else if (nout <= 48) basis_tc_t<48>(P_d, tiles_d, ntiles, s);
     else basis_tc_t<64>(P_d, tiles_d, ntiles, s);
+}
+
+// Ritz vectors of the converged problems on the tensor cores (ncv <= 64).
+// One shape serves every ncv: the kernel is bound by splitting V, whose
+// cost does not depend on the padded output count.  Measured on GB300
+// (4.1M rows, ncv 60): 25.3 ms for the FP64 kernel k_ritz.
+bool ritz_tc_fits(int max_ncv) { return max_ncv <= tc::NMAX && max_ncv <= tc::KMAX; }
+
+void launch_ritz_tc(const Problem *P_d, const Tile *tiles_d, int ntiles, cudaStream_t s) {
+    static std::atomic<unsigned long long> attr{0};
+    const size_t smem = basis_tc_smem<64>();
+    smem_limit_once(k_basis_tc<64, true>, (int)smem, attr);
+    prof_begin(s);
+    k_basis_tc<64, true><<<ntiles, tc::THREADS, smem, s>>>(P_d, tiles_d);
+    prof_end(KC_RITZ, s);
+    launch_counter() += 1;
+    variant_counter(HLANC_KL_RITZ_TC) += 1;
 }
 
 

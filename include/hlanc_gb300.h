@@ -292,7 +292,9 @@ long long hlanc_kernel_launches(void);
 #define HLANC_KL_BASIS_TC         5  /* restart basis update on the tensor cores */
 #define HLANC_KL_BASIS_FP64       6  /* restart basis update on FP64 CUDA cores */
 #define HLANC_KL_CYCLE            7  /* a whole Lanczos extension in one cooperative launch */
-#define HLANC_KL_KINDS            8
+#define HLANC_KL_RITZ_TC          8  /* Ritz vectors V Q2 on the tensor cores */
+#define HLANC_KL_RITZ_FP64        9  /* Ritz vectors V Q2 on FP64 CUDA cores */
+#define HLANC_KL_KINDS           10
 long long hlanc_kernel_launches_of(int kind);
 
 /* Per-kernel-class timing of the last solve run with opts.profile = 1 on the

@@ -263,6 +263,46 @@ def test_basis_fp64_path_beyond_tensor_core_shape(H):
     _check_pairs(m, vals, vecs, 20)
 
 
+def _dominant(n, k, seed=7):
+    # k well-separated dominant eigenvalues (1000, 950, ...) over a bulk in
+    # [0, 1), weak nearest-neighbour coupling: converges in the first
+    # extension, so no restart runs and both solves share V and Q2 exactly
+    rng = np.random.default_rng(seed)
+    d = np.concatenate([1000.0 - 50.0 * np.arange(k), rng.random(n - k)])[rng.permutation(n)]
+    rp, ci, va = [0], [], []
+    for i in range(n):
+        for j, x in ((i - 1, 1e-3), (i, d[i]), (i + 1, 1e-3)):
+            if 0 <= j < n:
+                ci.append(j)
+                va.append(x)
+        rp.append(len(ci))
+    return G.CSR(n, n, np.array(rp, dtype=np.int32), np.array(ci, dtype=np.int32), np.array(va))
+
+
+@pytest.mark.parametrize("n,nev,ncv", [(3000, 8, 24), (2000, 6, 64), (1000, 4, 12)])
+def test_ritz_vectors_tensor_cores_agree_with_fp64(H, n, nev, ncv):
+    # All ncv columns of V Q2 from the tensor-core kernel (FP64-exact digit
+    # splitting) and from the FP64 kernel, on the same V and Q2: no restart
+    # (no basis update) runs in either solve, so only the Ritz kernel differs.
+    m = _dominant(n, nev)
+    op = H.dcsrmv_operator_gpu(m)
+    before = H.variant_counts()
+    rc1, v1, x1, s1 = H.solve(op, nev, ncv, tol=1e-10)
+    mid = H.variant_counts()
+    rc2, v2, x2, s2 = H.solve(op, nev, ncv, tol=1e-10, basis_fp64=True)
+    after = H.variant_counts()
+    tc = {k: mid[k] - before[k] for k in before}
+    fp = {k: after[k] - mid[k] for k in before}
+    assert rc1 == rc2 == 0, (s1, s2)
+    assert tc["basis_tc"] == tc["basis_fp64"] == fp["basis_tc"] == fp["basis_fp64"] == 0, (tc, fp)
+    assert tc["ritz_tc"] == 1 and tc["ritz_fp64"] == 0, tc
+    assert fp["ritz_fp64"] == 1 and fp["ritz_tc"] == 0, fp
+    assert np.array_equal(v1, v2)
+    assert np.abs(x1 - x2).max() <= 1e-13 * np.abs(x2).max()
+    _check_pairs(m, v1, x1, nev)
+    assert np.abs(x1.T @ x1 - np.eye(ncv)).max() < 1e-12
+
+
 @pytest.mark.parametrize("case,gen,nev,ncv", [
     ("c1_laplacian2d_100", lambda: G.laplacian_2d(100), 10, 30),
     ("lap3d_12_shift", lambda: G.laplacian_3d(12, shift_seed=1), 20, 60),
