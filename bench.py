@@ -13,7 +13,11 @@ returned pair has ||A v - lambda v|| <= 1e-10 ||A||_inf.
             CUDA events on the solver's stream around K solves
     e2e     through the C ABI with pinned host buffers: dcsrmv_operator_gpu
             construction (CSR host->device) + ds_solver_gpu writing host
-            values/vectors (+ operator teardown), wall clock per solve
+            values/vectors (+ operator teardown), wall clock per solve,
+            median of --e2e-steps after one untimed call; run before the
+            other forms' matrices are generated on the host cores (that
+            generation slowed the 1.97 GB copy-out of the Ritz vectors from
+            11 ms to 160-410 ms)
     roofline  the dominant kernel class of one profiled solve (CUDA events
             around every launch): algorithmic bytes / time vs the measured
             HBM peak, and FP64 flops / time vs the live FP64 probe
@@ -777,7 +781,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="lap3d_160", choices=sorted(WORKLOADS))
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--full-spmv", type=int, default=0, help="SpMV count of a full solve (CPU extrapolation)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched / serving / mixed workloads")
@@ -815,14 +819,6 @@ def main():
     rank, world = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1)
     forms = not args.no_forms and world == 1 and rank == 0
     pool, pending = None, {}
-    if forms:
-        # the other forms' matrices, built on host cores while the GPU measures
-        import multiprocessing as mp
-        pool = mp.get_context("spawn").Pool(3)
-        pending = {"c3": pool.apply_async(_generate, ("c3", 0, 0)),
-                   "c4": pool.apply_async(_generate, ("c4", 512, 0)),
-                   "c5": pool.apply_async(_generate, ("c5", args.forms_serve_count, 2000000))}
-        pool.close()
 
     import torch
 
@@ -847,36 +843,6 @@ def main():
     for _ in range(args.warmup):
         st = solve_dev()
     torch.cuda.synchronize()
-    barrier(pg)
-    launches0 = H.kernel_launches()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    stats = []
-    with ClockSampler(dev) as clk:
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            stats.append(solve_dev())
-        e1.record(stream)
-        torch.cuda.synchronize()
-    launches = H.kernel_launches() - launches0
-    ms = e0.elapsed_time(e1) / args.steps
-    ms = allmax(pg, ms)
-    barrier(pg)
-    res, rdiff = H.residuals_device(op, nev, vals.data_ptr(), vecs.data_ptr(), m.n)
-    valid = all(s["rc"] == 0 and s["nconv"] >= nev for s in stats) and float(res.max()) <= 1e-10 * norm_a
-    value = replica_value(world, nev, ms) if valid else 0.0
-    parity = None
-    g = golden_of(args.workload)
-    if g is not None:
-        lam = vals[:nev].cpu().numpy()
-        ref = g["values"]
-        err = np.abs(lam - ref) / np.abs(ref)
-        parity = {"eigenvalue_rel_err_vs_reference_max": float(err.max()),
-                  "eigenvalue_rel_err_vs_reference": [float(x) for x in err],
-                  "reference_spmv_calls": int(g["spmv_calls"]),
-                  "reference": "the reference's own CPU solver (ds_solver_mkl + dcsrmv_operator_mkl) on the same "
-                               "matrix and start vector, tests/golden/%s.npz" % GOLDEN_OF[args.workload],
-                  "tolerance": 1e-10, "within_tolerance": bool(err.max() <= 1e-10)}
 
     # end to end through the C ABI with host buffers in pinned memory: the
     # operator is built from host CSR arrays, the solve returns its pairs to
@@ -894,8 +860,8 @@ def main():
         pinned(np.asarray(m.val, np.float64))
     values_h = torch.zeros(ncv, dtype=torch.float64, pin_memory=True).numpy()
     vectors_h = torch.zeros(m.n * ncv, dtype=torch.float64, pin_memory=True).numpy()
-    e2e_ms, e2e_parts = [], []
-    for _ in range(args.e2e_steps):
+    e2e_ms, e2e_parts, e2e_ok = [], [], True
+    for it in range(1 + args.e2e_steps):       # the first call is untimed (first use of the host buffers)
         torch.cuda.synchronize()
         t = time.perf_counter()
         op2 = H.dcsrmv_operator_gpu(hc, dev=dev, precision=prec)
@@ -906,13 +872,58 @@ def main():
         t2 = time.perf_counter()
         op2.close()
         t3 = time.perf_counter()
+        e2e_ok = e2e_ok and rc == 0
+        if it == 0:
+            continue
         e2e_ms.append((t3 - t) * 1e3)
         e2e_parts.append({"operator_create_ms": (t1 - t) * 1e3, "solve_and_copy_out_ms": (t2 - t1) * 1e3,
                           "operator_destroy_ms": (t3 - t2) * 1e3})
-        valid = valid and rc == 0
     e2e_ms = allmax(pg, statistics.median(e2e_ms))
     h2d = 4 * (m.n + 1) + 12 * m.nnz
     d2h = 8 * nev + 8 * m.n * ncv
+
+    if forms:
+        # the other forms' matrices, built on host cores while the GPU runs
+        # the device-timed solves (which do not touch host memory)
+        import multiprocessing as mp
+        pool = mp.get_context("spawn").Pool(3)
+        pending = {"c3": pool.apply_async(_generate, ("c3", 0, 0)),
+                   "c4": pool.apply_async(_generate, ("c4", 512, 0)),
+                   "c5": pool.apply_async(_generate, ("c5", args.forms_serve_count, 2000000))}
+        pool.close()
+
+    barrier(pg)
+    launches0 = H.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            stats.append(solve_dev())
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = H.kernel_launches() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = allmax(pg, ms)
+    barrier(pg)
+    res, rdiff = H.residuals_device(op, nev, vals.data_ptr(), vecs.data_ptr(), m.n)
+    valid = all(s["rc"] == 0 and s["nconv"] >= nev for s in stats) and float(res.max()) <= 1e-10 * norm_a
+    valid = valid and e2e_ok
+    value = replica_value(world, nev, ms) if valid else 0.0
+    parity = None
+    g = golden_of(args.workload)
+    if g is not None:
+        lam = vals[:nev].cpu().numpy()
+        ref = g["values"]
+        err = np.abs(lam - ref) / np.abs(ref)
+        parity = {"eigenvalue_rel_err_vs_reference_max": float(err.max()),
+                  "eigenvalue_rel_err_vs_reference": [float(x) for x in err],
+                  "reference_spmv_calls": int(g["spmv_calls"]),
+                  "reference": "the reference's own CPU solver (ds_solver_mkl + dcsrmv_operator_mkl) on the same "
+                               "matrix and start vector, tests/golden/%s.npz" % GOLDEN_OF[args.workload],
+                  "tolerance": 1e-10, "within_tolerance": bool(err.max() <= 1e-10)}
+
 
     # the SpMV kernel alone (dcsrmv_operator_gpu::operator() on device vectors)
     xs = torch.rand(m.n, dtype=torch.float64, device="cuda")
