@@ -85,6 +85,73 @@ __device__ __forceinline__ void reduce_all(const double *src, int nb, int nv, do
 
 struct CycTile { int prob, rank, nb, row0, row1, pad; };
 
+// One panel of the projection: columns c0 .. c0 + CC (CC <= 8) of V
+// against w over the CTA's rows, per-thread sums, then one transposed warp
+// reduction into wsum[warp][column].  CC is a compile-time count, so no FP64
+// instruction is issued for an absent column (predicated-off FP64
+// instructions still occupy GB300's narrow FP64 pipe).  Every present
+// column's sum is formed in the same order whatever CC is.
+template <int CC>
+__device__ __forceinline__ void cyc_proj_panel(const double *__restrict__ V, size_t ld, int c0, int row0, int row1,
+                                               const double *__restrict__ w, double (*wsum)[MAXNCV + 1]) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    double a[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) a[q] = 0.0;
+    for (int r = row0 + tid; r < row1; r += CTPB) {
+        const double wr = w[r];
+        const double *vr = V + (size_t)c0 * ld + r;
+        double va[CC];
+#pragma unroll
+        for (int q = 0; q < CC; ++q) va[q] = vr[(size_t)q * ld];
+#pragma unroll
+        for (int q = 0; q < CC; ++q) a[q] = fma(va[q], wr, a[q]);
+    }
+    const int q = lane >> 2;
+    const double v = warp_reduce8(a);
+    if ((lane & 3) == 0 && q < CC) wsum[warp][c0 + q] = v;
+}
+
+__device__ __forceinline__ void cyc_proj_panel_n(int cc, const double *__restrict__ V, size_t ld, int c0, int row0,
+                                                 int row1, const double *__restrict__ w, double (*wsum)[MAXNCV + 1]) {
+    switch (cc) {
+    case 1: cyc_proj_panel<1>(V, ld, c0, row0, row1, w, wsum); break;
+    case 2: cyc_proj_panel<2>(V, ld, c0, row0, row1, w, wsum); break;
+    case 3: cyc_proj_panel<3>(V, ld, c0, row0, row1, w, wsum); break;
+    case 4: cyc_proj_panel<4>(V, ld, c0, row0, row1, w, wsum); break;
+    case 5: cyc_proj_panel<5>(V, ld, c0, row0, row1, w, wsum); break;
+    case 6: cyc_proj_panel<6>(V, ld, c0, row0, row1, w, wsum); break;
+    case 7: cyc_proj_panel<7>(V, ld, c0, row0, row1, w, wsum); break;
+    default: cyc_proj_panel<8>(V, ld, c0, row0, row1, w, wsum); break;
+    }
+}
+
+// acc -= V[r, k .. k + R) h[k .. k + R), loads first, in column order.
+template <int R>
+__device__ __forceinline__ double cyc_update_fp64(const double *__restrict__ vr, size_t ld, int k, const double *hs,
+                                                  double acc) {
+    double v[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = vr[(size_t)(k + q) * ld];
+#pragma unroll
+    for (int q = 0; q < R; ++q) acc = fma(-v[q], hs[k + q], acc);
+    return acc;
+}
+
+__device__ __forceinline__ double cyc_update_fp64_n(int cnt, const double *__restrict__ vr, size_t ld, int k,
+                                                    const double *hs, double acc) {
+    switch (cnt) {
+    case 1: return cyc_update_fp64<1>(vr, ld, k, hs, acc);
+    case 2: return cyc_update_fp64<2>(vr, ld, k, hs, acc);
+    case 3: return cyc_update_fp64<3>(vr, ld, k, hs, acc);
+    case 4: return cyc_update_fp64<4>(vr, ld, k, hs, acc);
+    case 5: return cyc_update_fp64<5>(vr, ld, k, hs, acc);
+    case 6: return cyc_update_fp64<6>(vr, ld, k, hs, acc);
+    case 7: return cyc_update_fp64<7>(vr, ld, k, hs, acc);
+    default: return cyc_update_fp64<8>(vr, ld, k, hs, acc);
+    }
+}
+
 template <bool F32>
 __device__ __forceinline__ double cyc_spmv_row(const Problem &P, const double *__restrict__ rin, double t1, int r) {
     const int a = P.row_ptr[r], b = P.row_ptr[r + 1];
@@ -179,32 +246,36 @@ __global__ void __launch_bounds__(CTPB) k_cycle(const Problem *__restrict__ prob
             double nrm = 0.0;
             if (norm)
                 for (int r = row0 + tid; r < row1; r += CTPB) nrm = fma(w[r], w[r], nrm);
-            for (int c0 = 0; c0 < c; c0 += 16) {       // two panels of 8 per round
+            int c0 = 0;
+            for (; c0 + 16 <= c; c0 += 16) {          // full rounds: two panels of 8
                 double a[8], b[8];
 #pragma unroll
                 for (int q = 0; q < 8; ++q) a[q] = b[q] = 0.0;
-                const int cc = min(16, c - c0);
                 for (int r = row0 + tid; r < row1; r += CTPB) {
                     const double wr = w[r];
                     const double *vr = P.V + (size_t)c0 * ld + r;
                     double va[8], vb[8];
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
-                        va[q] = q < cc ? vr[(size_t)q * ld] : 0.0;
-                        vb[q] = q + 8 < cc ? vr[(size_t)(q + 8) * ld] : 0.0;
+                        va[q] = vr[(size_t)q * ld];
+                        vb[q] = vr[(size_t)(q + 8) * ld];
                     }
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
-                        if (q < cc) a[q] = fma(va[q], wr, a[q]);
-                        if (q + 8 < cc) b[q] = fma(vb[q], wr, b[q]);
+                        a[q] = fma(va[q], wr, a[q]);
+                        b[q] = fma(vb[q], wr, b[q]);
                     }
                 }
                 const double v = warp_reduce8(a);
                 const double u = warp_reduce8(b);
                 const int q = lane >> 2;
-                if ((lane & 3) == 0 && q < cc) wsum[warp][c0 + q] = v;
-                if ((lane & 3) == 0 && q + 8 < cc) wsum[warp][c0 + 8 + q] = u;
+                if ((lane & 3) == 0) {
+                    wsum[warp][c0 + q] = v;
+                    wsum[warp][c0 + 8 + q] = u;
+                }
             }
+            for (; c0 < c; c0 += 8)                     // the rest, panels of exactly the remaining columns
+                cyc_proj_panel_n(min(8, c - c0), P.V, ld, c0, row0, row1, w, wsum);
             if (norm) {
                 nrm = warp_sum(nrm);
                 if (lane == 0) wsum[warp][c] = nrm;
@@ -271,14 +342,8 @@ __global__ void __launch_bounds__(CTPB) k_cycle(const Problem *__restrict__ prob
                         if (i0 + q < tf) a32 = fmaf(v[q], h32s[i0 + q], a32);
                 }
                 acc = fma(-(double)a32, unscale, acc);
-                for (int i0 = tf; i0 < c; i0 += 8) {
-                    double v[8];
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) v[q] = i0 + q < c ? P.V[(size_t)(i0 + q) * ld + r] : 0.0;
-#pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        if (i0 + q < c) acc = fma(-v[q], hs[i0 + q], acc);
-                }
+                for (int i0 = tf; i0 < c; i0 += 8)
+                    acc = cyc_update_fp64_n(min(8, c - i0), P.V + r, ld, i0, hs, acc);
                 w[r] = acc;
                 nrm2 = fma(acc, acc, nrm2);
             }
