@@ -1368,6 +1368,7 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
     State S = S1;
     bool accepted = false;             // the refined FP32-phase pairs are the result
     double rr_resid = -1.0;
+    double copy_s = 0.0;               // host outputs: the copy-out of the pairs
     if (fp32) {
         // FP64 Rayleigh-Ritz of the FP32 phase's pairs; FP64 restart cycles
         // from the refined vectors where a residual misses the tolerance
@@ -1411,10 +1412,13 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
             CK(cudaMemcpy2DAsync(vectors, sizeof(double) * (size_t)ldv, p.vout, sizeof(double) * (size_t)p.ldo,
                                  sizeof(double) * (size_t)n, m, cudaMemcpyDeviceToDevice, E.stream));
         } else {
+            CK(cudaStreamSynchronize(E.stream));
+            const double tc = now_s();
             CK(cudaMemcpyAsync(values, p.small + SM_VALS(m), sizeof(double) * nconv, cudaMemcpyDeviceToHost, E.stream));
             if ((rc = copy_d2h_2d(vectors, sizeof(double) * (size_t)ldv, p.vout, sizeof(double) * (size_t)p.ldo,
                                   sizeof(double) * (size_t)n, m, E.stream)))
                 return rc;
+            copy_s = now_s() - tc;
         }
         CK(cudaStreamSynchronize(E.stream));
     } else if (S.status == ST_CONVERGED) {
@@ -1433,17 +1437,23 @@ int solve_one(int dev, int n, int nev, int ncv, double *values, double *vectors,
             if (device_out) {
                 CK(cudaMemcpyAsync(values, p.small + SM_VALS(m), sizeof(double) * nconv, cudaMemcpyDeviceToDevice, E.stream));
             } else {
+                CK(cudaStreamSynchronize(E.stream));
+                const double tc = now_s();
                 CK(cudaMemcpyAsync(values, p.small + SM_VALS(m), sizeof(double) * nconv, cudaMemcpyDeviceToHost, E.stream));
                 if ((rc = copy_d2h_2d(vectors, sizeof(double) * (size_t)ldv, p.vout, sizeof(double) * (size_t)p.ldo,
                                       sizeof(double) * (size_t)n, m, E.stream)))
                     return rc;
+                copy_s = now_s() - tc;
             }
             CK(cudaStreamSynchronize(E.stream));
         }
     }
     const double nnz = csr ? (double)csr->nnz : 0.0;
     fill_stats(stats, S, p, nnz, fp32 ? 1 : 0, refine_restarts, now_s() - t0, status);
-    if (stats) stats->refine_residual = rr_resid;
+    if (stats) {
+        stats->refine_residual = rr_resid;
+        stats->copy_out_seconds = copy_s;
+    }
     if (stats && S.status == ST_CONVERGED) stats->bytes_restart += 16.0 * n * ncv;
     fill_profile(S, p, nnz, fp32 ? 1 : 0);
     return status;
@@ -1572,12 +1582,32 @@ int hlanc_csr_create(int dev, int nrows, int ncols, int nnz, const int *row_ptr,
         return HLANC_ERR_INVALID;
     if (precision != HLANC_PREC_FP64 && precision != HLANC_PREC_FP32_REFINE) return HLANC_ERR_INVALID;
     if (row_ptr[0] != 0) return HLANC_ERR_INVALID;
-    for (int r = 0; r < nrows; ++r)
-        if (row_ptr[r + 1] < row_ptr[r]) return HLANC_ERR_INVALID;
+    // The checks and the norm scan over row chunks on the host worker pool
+    // (a 4.1M-row, 28.5M-entry matrix is ~30 ms of one core): row_ptr is
+    // checked everywhere before any chunk reads col through it.
+    const int nchunk = nrows >= (1 << 16) ? 64 : 1;
+    auto chunk_rows = [&](int q, int &r0, int &r1) {
+        r0 = (int)((long long)nrows * q / nchunk);
+        r1 = (int)((long long)nrows * (q + 1) / nchunk);
+    };
+    std::vector<int> bad(nchunk, 0);
+    HostPool::get().run(nchunk, [&](int q) {
+        int r0, r1;
+        chunk_rows(q, r0, r1);
+        for (int r = r0; r < r1; ++r)
+            if (row_ptr[r + 1] < row_ptr[r]) { bad[q] = 1; return; }
+    });
+    for (int q = 0; q < nchunk; ++q)
+        if (bad[q]) return HLANC_ERR_INVALID;
     if (row_ptr[nrows] > nnz) return HLANC_ERR_INVALID;
-    const int used = row_ptr[nrows];
-    for (int i = 0; i < used; ++i)
-        if (col[i] < 0 || col[i] >= ncols) return HLANC_ERR_INVALID;
+    HostPool::get().run(nchunk, [&](int q) {
+        int r0, r1;
+        chunk_rows(q, r0, r1);
+        for (int i = row_ptr[r0]; i < row_ptr[r1]; ++i)
+            if (col[i] < 0 || col[i] >= ncols) { bad[q] = 1; return; }
+    });
+    for (int q = 0; q < nchunk; ++q)
+        if (bad[q]) return HLANC_ERR_INVALID;
     // general CSR on the device: symmetric-lower input is mirrored (only
     // entries with col <= row are used, as cuSPARSE SYMMETRIC / mkl "SLNC" do)
     std::vector<int> rp, ci;
@@ -1610,16 +1640,24 @@ int hlanc_csr_create(int dev, int nrows, int ncols, int nnz, const int *row_ptr,
     const long long gnnz = grp[nrows];
     std::unique_ptr<hlanc_csr_s> h(new hlanc_csr_s());
     h->dev = dev; h->nrows = nrows; h->ncols = ncols; h->precision = precision; h->nnz = gnnz;
-    double ninf = 0.0;
-    long long mrow = 0;
-    for (int r = 0; r < nrows; ++r) {
-        double s = 0.0;
-        for (int i = grp[r]; i < grp[r + 1]; ++i) s += fabs(gva[i]);
-        ninf = std::max(ninf, s);
-        mrow = std::max<long long>(mrow, grp[r + 1] - grp[r]);
-    }
-    h->norm_inf = ninf;
-    h->max_row = mrow;
+    std::vector<double> cn(nchunk, 0.0);
+    std::vector<long long> cm(nchunk, 0);
+    HostPool::get().run(nchunk, [&](int q) {
+        int r0, r1;
+        chunk_rows(q, r0, r1);
+        double ninf = 0.0;
+        long long mrow = 0;
+        for (int r = r0; r < r1; ++r) {
+            double s = 0.0;
+            for (int i = grp[r]; i < grp[r + 1]; ++i) s += fabs(gva[i]);
+            ninf = std::max(ninf, s);
+            mrow = std::max<long long>(mrow, grp[r + 1] - grp[r]);
+        }
+        cn[q] = ninf;
+        cm[q] = mrow;
+    });
+    h->norm_inf = *std::max_element(cn.begin(), cn.end());
+    h->max_row = *std::max_element(cm.begin(), cm.end());
     build_spmv_tiles(grp, nrows, h->stiles_h);
     DevGuard g(dev);
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));

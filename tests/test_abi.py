@@ -62,6 +62,37 @@ def test_cgs_diag_rejects_bad_arguments(H):
     assert f(0, 4096, 8, H.HLANC_CGS_FP64, 1, None) == bad
 
 
+def test_operator_rejects_bad_csr_before_any_cuda_call(H):
+    # 2^17 rows: the checks run in row chunks on the host worker pool; a bad
+    # row pointer or column index in any chunk is found before device memory
+    # is touched (HLANC_ERR_INVALID), and a valid matrix gets past them
+    n = 1 << 17
+    rp = (np.arange(n + 1) * 2).astype(np.int32)
+    col = np.stack([np.arange(n), (np.arange(n) + 1) % n], axis=1).reshape(-1).astype(np.int32)
+    val = np.ones(2 * n)
+    f = H.lib().hlanc_csr_create
+
+    def create(rp_, col_, nnz):
+        h = C.c_void_p()
+        rc = f(0, n, n, nnz, rp_.ctypes.data, col_.ctypes.data, val.ctypes.data, 0, H.HLANC_PREC_FP64, C.byref(h))
+        if rc == 0:
+            H.lib().hlanc_csr_destroy(h)
+        return rc
+
+    bad = 2                                                         # HLANC_ERR_INVALID
+    r = rp.copy()
+    r[n - 5] = r[n - 6] - 1                                         # decreasing, in the last chunk
+    assert create(r, col, 2 * n) == bad
+    c = col.copy()
+    c[-3] = n                                                       # column out of range, last chunk
+    assert create(rp, c, 2 * n) == bad
+    c = col.copy()
+    c[7] = -1                                                       # negative column, first chunk
+    assert create(rp, c, 2 * n) == bad
+    assert create(rp, col, 2 * n - 1) == bad                        # row_ptr[n] > nnz
+    assert create(rp, col, 2 * n) in (0, 3)                         # ok, or no device here (HLANC_ERR_CUDA)
+
+
 def test_status_strings(H):
     assert H.lib().hlanc_status_string(0) == b"ok"
     assert H.lib().hlanc_status_string(1) == b"not converged"
