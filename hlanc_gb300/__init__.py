@@ -63,7 +63,7 @@ class Stats(C.Structure):
                 ("nconv", C.c_int), ("refine_restarts", C.c_int), ("status", C.c_int),
                 ("rnorm", C.c_double), ("seconds", C.c_double), ("bytes_spmv", C.c_double),
                 ("bytes_cgs", C.c_double), ("bytes_restart", C.c_double), ("cgs_update_fp32_share", C.c_double),
-                ("refine_residual", C.c_double), ("reserved", C.c_double * 2)]
+                ("refine_residual", C.c_double), ("copy_out_seconds", C.c_double), ("reserved", C.c_double * 1)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

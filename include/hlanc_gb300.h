@@ -168,7 +168,8 @@ typedef struct {
     double refine_residual;   /* mixed precision: largest ||A y - theta y|| / ||A||_inf after the
                                  FP64 Rayleigh-Ritz of the FP32 phase's pairs (-1: not run); the
                                  pairs were accepted as they are when refine_restarts == 0 */
-    double reserved[2];
+    double copy_out_seconds;  /* host outputs: wall time of the device-to-host copy of the pairs */
+    double reserved[1];
 } hlanc_stats_t;
 
 /* ds_solver_gpu(n, nev, ncv, values, vectors, ldv, op, dev): largest
