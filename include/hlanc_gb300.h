@@ -40,10 +40,11 @@ extern "C" {
                                         operator, accepted when every FP64 residual meets tol,
                                         else FP64 restart cycles from the refined vectors */
 
-/* Kernel of the restart's basis update V <- V Q (hlanc_opts_t.basis_kernel). */
+/* Kernel of the restart's basis update V <- V Q and of the final Ritz
+ * vectors V Q2 (hlanc_opts_t.basis_kernel). */
 #define HLANC_BASIS_AUTO          0  /* tensor cores (FP64-accurate integer splitting) when
-                                        ncv <= 64 (so nev <= 63), else the FP64 kernel */
-#define HLANC_BASIS_FP64          1  /* always the FP64 CUDA-core kernel */
+                                        ncv <= 64 (so nev <= 63), else the FP64 kernels */
+#define HLANC_BASIS_FP64          1  /* always the FP64 CUDA-core kernels */
 
 /* Arithmetic of the CGS passes h = V^T w, w -= V h (hlanc_opts_t.cgs_kernel).
  * The hybrid projection runs 5 of every 8 columns as FP64 FMAs and 3 as
