@@ -603,7 +603,14 @@ public:
     int ntiles = 0, nslots_cap = 0, ntiles_cap = 0, nstiles = 0, nstiles_cap = 0;
     int max_ncv = 0;
     bool fp32_any = false;
-    std::map<long long, cudaGraphExec_t> graphs;
+    // A captured cycle and the kernels it holds (total and per counted
+    // variant), added to the launch counters on every replay.
+    struct Captured {
+        cudaGraphExec_t exec = nullptr;
+        long long kernels = 0;
+        long long variants[HLANC_KL_KINDS] = {};
+    };
+    std::map<long long, Captured> graphs;
     // host-restart mailbox
     std::vector<long long> off_h;
     long long *off_d = nullptr;
@@ -650,7 +657,7 @@ public:
     }
 
     void drop_graphs() {
-        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+        for (auto &kv : graphs) cudaGraphExecDestroy(kv.second.exec);
         graphs.clear();
     }
 
@@ -943,17 +950,27 @@ public:
             const long long key = (long long)steps * 1024 + basis_bucket(basis_nev);
             auto it = graphs.find(key);
             if (it == graphs.end()) {
+                // the enqueue counts the captured kernels once, for this
+                // first replay
+                Captured c;
+                long long v0[HLANC_KL_KINDS];
+                for (int k = 0; k < HLANC_KL_KINDS; ++k) v0[k] = variant_counter(k).load();
+                const long long k0 = launch_counter().load();
                 cudaGraph_t g;
                 CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
                 enqueue_cycle(steps, basis_nev);
                 CK(cudaStreamEndCapture(stream, &g));
-                cudaGraphExec_t ge;
-                cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+                c.kernels = launch_counter().load() - k0;
+                for (int k = 0; k < HLANC_KL_KINDS; ++k) c.variants[k] = variant_counter(k).load() - v0[k];
+                cudaError_t e = cudaGraphInstantiate(&c.exec, g, 0);
                 cudaGraphDestroy(g);
                 CK(e);
-                it = graphs.emplace(key, ge).first;
+                it = graphs.emplace(key, c).first;
+            } else {
+                launch_counter() += it->second.kernels;
+                for (int k = 1; k < HLANC_KL_KINDS; ++k) variant_counter(k) += it->second.variants[k];
             }
-            CK(cudaGraphLaunch(it->second, stream));
+            CK(cudaGraphLaunch(it->second.exec, stream));
         }
         for (size_t a = 0; a < active.size(); ++a) probs[active[a]].cycles += 1;
         return pull_mailbox();

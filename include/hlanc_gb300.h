@@ -281,7 +281,8 @@ int hlanc_server_stats(hlanc_server_t s, hlanc_server_stats_t *out);
 int hlanc_server_destroy(hlanc_server_t s);
 
 /* ---- diagnostics ---------------------------------------------------------- */
-/* Number of kernels this library launched since load (all devices). */
+/* Number of kernels this library launched since load (all devices); every
+ * kernel of a replayed CUDA graph counts, as if launched one by one. */
 long long hlanc_kernel_launches(void);
 
 /* Launches since load of one kernel variant (no reference counterpart; tests

@@ -227,11 +227,16 @@ def test_invalid_arguments(H):
 def test_graph_and_eager_agree(H):
     m = G.laplacian_2d(50)
     op = H.dcsrmv_operator_gpu(m)
+    k0 = H.kernel_launches()
     rc1, v1, _, s1 = H.solve(op, 8, 24, use_graphs=True)
+    k1 = H.kernel_launches()
     rc2, v2, _, s2 = H.solve(op, 8, 24, use_graphs=False)
+    k2 = H.kernel_launches()
     assert rc1 == rc2 == 0
     assert np.array_equal(v1, v2)                  # same kernels, same order: bit-identical
     assert s1["spmv_calls"] == s2["spmv_calls"]
+    # replayed graphs count their kernels like eager launches
+    assert k1 - k0 == k2 - k1 > 0, (k1 - k0, k2 - k1)
 
 
 @pytest.mark.parametrize("gen,nev,ncv", [
