@@ -880,7 +880,7 @@ def main():
         if cudart is None:
             return None, torch.zeros(count, dtype=torch.float64, pin_memory=True).numpy()
         p = ctypes.c_void_p()
-        if cudart.cudaHostAlloc(ctypes.byref(p), ctypes.c_size_t(8 * count), 1) != 0:   # portable
+        if cudart.cudaHostAlloc(ctypes.byref(p), ctypes.c_size_t(8 * count), 3) != 0:   # portable | mapped
             raise RuntimeError("cudaHostAlloc failed")
         a = np.ctypeslib.as_array((ctypes.c_double * count).from_address(p.value))
         a[...] = 0.0

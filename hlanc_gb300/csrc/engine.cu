@@ -1248,18 +1248,57 @@ __global__ void k_sum_columns(const double *__restrict__ Y, int ld, int n, int k
 
 int map_status(int st) { return st == ST_CONVERGED ? HLANC_OK : HLANC_NOT_CONVERGED; }
 
-// Device -> host copy of `height` columns of `width` bytes, synchronous.  A
-// large pageable destination (the reference API's `new double[]`) is
-// page-locked for the copy, so it runs as one DMA instead of a staged
-// pageable copy (measured on GB300: 2 GB of Ritz vectors in 1.65 s staged).
+// Column-by-column copy through the device's address space (blockIdx.y =
+// column, w elements of T per column).
+template <typename T>
+__global__ void __launch_bounds__(256) k_copy_cols(const T *__restrict__ src, size_t sp, T *__restrict__ dst,
+                                                   size_t dp, size_t w) {
+    const T *c = src + (size_t)blockIdx.y * sp;
+    T *d = dst + (size_t)blockIdx.y * dp;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < w; i += (size_t)gridDim.x * blockDim.x)
+        d[i] = c[i];
+}
+
+// Device -> host copy of `height` columns of `width` bytes, synchronous.
+//  - A large pinned destination that is mapped into this device's address
+//    space is written by a copy kernel.  Measured on this machine's GB300
+//    machines (1.97 GB of Ritz vectors): the DMA copy took 10 ms on a quiet
+//    host but 130-230 ms inside some solver processes, where stores from
+//    the SMs into the same kind of buffer took 34 ms; on a quiet host the
+//    kernel copy takes 10 ms like the DMA.
+//  - A large pageable destination (the reference API's `new double[]`) is
+//    page-locked for the copy, so it runs as one DMA instead of a staged
+//    pageable copy (2 GB of Ritz vectors in 1.65 s staged).
 int copy_d2h_2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
                 cudaStream_t s) {
     const size_t span = height ? dpitch * (height - 1) + width : 0;
     bool registered = false;
     if (span >= ((size_t)64 << 20)) {
         cudaPointerAttributes a;
-        if (cudaPointerGetAttributes(&a, dst) == cudaSuccess && a.type == cudaMemoryTypeUnregistered)
-            registered = cudaHostRegister(dst, span, cudaHostRegisterDefault) == cudaSuccess;
+        int dev = -1;
+        cudaGetDevice(&dev);
+        if (cudaPointerGetAttributes(&a, dst) == cudaSuccess) {
+            const uintptr_t dp = (uintptr_t)a.devicePointer, sp = (uintptr_t)src;
+            if (a.type == cudaMemoryTypeHost && dp && a.device == dev && height <= 65535 &&
+                ((width | dpitch | spitch | dp | sp) & 7) == 0) {
+                const unsigned gx = (unsigned)std::max<size_t>(1, (size_t)1216 / height);
+                const dim3 grid(gx, (unsigned)height);
+                if (((width | dpitch | spitch | dp | sp) & 15) == 0)
+                    k_copy_cols<double2><<<grid, 256, 0, s>>>(static_cast<const double2 *>(src), spitch / 16,
+                                                              reinterpret_cast<double2 *>(dp), dpitch / 16,
+                                                              width / 16);
+                else
+                    k_copy_cols<double><<<grid, 256, 0, s>>>(static_cast<const double *>(src), spitch / 8,
+                                                             reinterpret_cast<double *>(dp), dpitch / 8, width / 8);
+                launch_counter() += 1;
+                cudaError_t e = cudaGetLastError();
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+                CK(e);
+                return HLANC_OK;
+            }
+            if (a.type == cudaMemoryTypeUnregistered)
+                registered = cudaHostRegister(dst, span, cudaHostRegisterDefault) == cudaSuccess;
+        }
         cudaGetLastError();   // an unregistrable range only means the staged copy
     }
     cudaError_t e = cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, cudaMemcpyDeviceToHost, s);

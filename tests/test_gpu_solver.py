@@ -478,3 +478,34 @@ def test_native_library_loaded(H):
         maps = f.read()
     assert os.path.basename(H.LIB_PATH) in maps
     assert H.kernel_launches() > 0
+
+
+def test_host_outputs_pinned_and_pageable_agree(H):
+    # Outputs above 64 MB: a pinned host buffer (mapped into the device's
+    # address space) is written by the library's copy kernel, 16-byte and
+    # 8-byte forms (even and odd ldv); a pageable one is page-locked and
+    # copied by DMA.  Same pairs, bit for bit.
+    import torch
+    m = G.laplacian_3d(60, shift_seed=1)          # 216,000 rows; 40 columns = 69 MB
+    op = H.dcsrmv_operator_gpu(m)
+    nev, ncv = 10, 40
+    out = {}
+    for kind, ldv in (("pageable", m.n), ("pinned", m.n), ("pinned", m.n + 1)):
+        values = np.zeros(ncv)
+        if kind == "pinned":
+            vectors = torch.zeros(ldv * ncv, dtype=torch.float64, pin_memory=True).numpy()
+        else:
+            vectors = np.zeros(ldv * ncv)
+        vectors[:] = 7.0
+        st = {}
+        rc = H.ds_solver_gpu(m.n, nev, ncv, values, vectors, ldv, op, opts_=H.opts(tol=1e-10), stats=st)
+        assert rc == 0, st
+        X = vectors.reshape(ncv, ldv).T
+        if ldv > m.n:
+            assert np.all(X[m.n:, :] == 7.0)       # padding rows untouched
+        out[(kind, ldv)] = (values.copy(), np.ascontiguousarray(X[: m.n, :]))
+    ref_v, ref_x = out[("pageable", m.n)]
+    for key, (v, x) in out.items():
+        assert np.array_equal(v, ref_v), key
+        assert np.array_equal(x, ref_x), key
+    _check_pairs(m, ref_v, ref_x, nev)
