@@ -30,3 +30,17 @@ def test_reference_arm_json_line():
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+
+
+def test_roofline_inputs_from_committed_profiles():
+    # the GPU arm's roofline takes the DRAM/algorithmic traffic ratio of the
+    # dominant CGS kernel from the committed ncu summaries, and the FP64
+    # share of the hybrid projection from its 5 + 3 panel split
+    sys.path.insert(0, ROOT)
+    import bench
+    for k in ("cgs_proj", "cgs_apply"):
+        r = bench.read_traffic_ratio(k)
+        assert r is not None and 0.8 < r < 1.3, (k, r)
+    s = bench.cgs_fp64_share("cgs_proj", 20, 60)
+    assert 0.6 < s < 0.65, s
+    assert bench.cgs_fp64_share("cgs_proj", 7, 8) == 5 / 8   # one full panel
